@@ -1,0 +1,360 @@
+"""Benchmark: grid-point RK3 steps per second of the Littleharsh time step.
+
+Workload (configuration 2 of the benchmark set, the production FP64 drop-in on
+one GPU): Re_b = 10000 (Re_tau ~ 550), Lx = 2pi, Lz = pi, 576 x 576 dealiased
+physical points (384 x 384 Fourier modes), ny = 385 stretched points plus 32
+canopy points per wall (450 u levels), 48 x 24 square posts per wall,
+h = 0.1, 8 x 8 points per post; seeded laminar + 10% perturbation field,
+projected divergence free; fixed dt from CFL 0.5.  FP64 throughout.
+
+Metric: Ngal_x * Ngal_z * Ny_u * steps / second (whole job: summed over the
+replicas of all ranks).  A "step" is one full RK3 step (three substages).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU FP64 restatement of the reference's step (the
+Fortran reference cannot be built here) on the host cores, on a bounded
+sample: one RK3 step of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "config2_576x576x450_fp64": dict(Re=10000.0, alp=1.0, bet=2.0, ngalx=576, ngalz=576, ny=385, dyq=13.6, ppp=5,
+                                     geometry_type=3, posth=0.1, dsty=32, dstx=8, dstz=8, ntilex=48, ntilez=24,
+                                     flag_ctpress=0),
+    "config1_96x96x130_fp64": dict(Re=2800.0, alp=1.0, bet=2.0, ngalx=96, ngalz=96, ny=97, dyq=13.6, ppp=5,
+                                   geometry_type=3, posth=0.2, dsty=16, dstx=2, dstz=4, ntilex=12, ntilez=6,
+                                   flag_ctpress=0),
+}
+DEFAULT_WORKLOAD = "config2_576x576x450_fp64"
+METRIC = "grid-pt RK3 steps/s"
+UNIT = "grid-pt steps/s"
+BYTES_PER_POINT_FP64 = 576  # compulsory state traffic per spectral point per RK3 step
+
+
+def _peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    out = {"hbm_gbs": 6800.0, "src": "fallback"}
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            out = {"hbm_gbs": float(d["hbm_gbs"]), "src": "measured"}
+        except Exception:
+            pass
+    # FP64 FMA peak of this machine's GB300 (own probe: 8 independent FMA chains per
+    # thread, 1216 CTAs x 256 threads, CUDA events): 1.198 TFLOP/s
+    out["fp64_tflops"] = 1.198
+    return out
+
+
+# ----------------------------------------------------------------------------
+# clocks during the timed region
+# ----------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------
+# model counts for the roofline
+# ----------------------------------------------------------------------------
+def _stages(n: int):
+    m, n4, n2, n3 = n, 0, 0, 0
+    while m % 4 == 0:
+        m //= 4
+        n4 += 1
+    while m % 2 == 0:
+        m //= 2
+        n2 += 1
+    while m % 3 == 0:
+        m //= 3
+        n3 += 1
+    return [3] * n3 + [2] * n2 + [4] * n4
+
+
+def fft_flops(n: int) -> float:
+    """Real FP64 operations (FMA = 2) of one complex DIF of length n as the kernels
+    execute it: per butterfly r=4: 16 + 18 twiddle, r=2: 4 + 6, r=3: 16 + 12; the
+    last stage has no twiddles."""
+    rad = _stages(n)
+    tot = 0.0
+    for s, r in enumerate(rad):
+        last = s == len(rad) - 1
+        base = {4: 16, 2: 4, 3: 16}[r]
+        tw = 0 if last else {4: 18, 2: 6, 3: 12}[r]
+        tot += (n / r) * (base + tw)
+    return tot
+
+
+def xprod_flops(ngx, ngz, nkx, nlev) -> float:
+    """x-pass with products for one substage: per level and z row, 3 inverse
+    and 6 forward real transforms (complex DIF of ngx/2 plus pre/post
+    processing), interpolation and products."""
+    h = ngx // 2
+    inv = fft_flops(h) + 12.0 * h
+    fwd = fft_flops(h) + 18.0 * nkx
+    prod = ngx * (6 + 3 * 3)
+    return nlev * ngz * (3 * inv + 6 * fwd + prod)
+
+
+def z_flops(ngz, nkx, nplanes) -> float:
+    return nplanes * nkx * fft_flops(ngz)
+
+
+# ----------------------------------------------------------------------------
+def build_solver(cfg: dict, precision: int, seed: int):
+    import littleharsh_gb300 as lh
+    from littleharsh_gb300.initial import initial_field
+    s = lh.Solver(lh.Config(**cfg), precision=precision)
+    g = s.grid
+    u1, u2, u3, p = initial_field(g["yu"], g["yv"], s.nz, s.nkx, s.nyp, seed=seed)
+    s.set_fields(u1, u2, u3, p)
+    s.project()
+    dt = s.cfl_dt(0.5)
+    s.set_time(0.0, dt, 0.0)
+    return s, (u1, u2, u3, p)
+
+
+def cpu_baseline(cfg: dict, threads: int) -> dict:
+    """The CPU FP64 restatement on the host cores: one RK3 step of the workload."""
+    from oracle import pyoracle
+    from littleharsh_gb300.initial import initial_field
+    pyoracle.build()
+    o = pyoracle.Oracle(**cfg, nthreads=threads)
+    g = o.grid()
+    o.set_fields(*initial_field(g["yu"], g["yv"], o.nz, o.nkx, o.nyp, seed=1))
+    o.set_scalars(0.0, 1.0, 0.0)
+    o.project()
+    o.set_scalars(0.0, o.cfl_dt(0.5), 0.0, o.flowrate())
+    t0 = time.perf_counter()
+    o.step(1)
+    sec = time.perf_counter() - t0
+    pts = o.ngx * o.ngz * o.nyu
+    return {"value": pts / sec, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"1 RK3 step of {cfg['ngalx']}x{cfg['ngalz']}x{o.nyu} FP64 ({sec:.1f} s)"}
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    cfg = WORKLOADS[args.workload]
+    threads = os.cpu_count() or 1
+    vals = []
+    base = None
+    for _ in range(max(args.warmup, 0)):
+        pass  # the oracle has no warm-up effects worth a full extra step of CPU time
+    for _ in range(max(1, min(args.steps, 2))):
+        base = cpu_baseline(cfg, threads)
+        vals.append(base["value"])
+    v = statistics.median(vals)
+    base["value"] = v
+    pts = cfg["ngalx"] * cfg["ngalz"] * (cfg["ny"] + 2 * cfg["dsty"] + 1)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": len(vals),
+            "warmup": args.warmup, "ms_per_step": 1e3 * pts / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded laminar + perturbation field)",
+            "config": {"workload": args.workload, "grid": [cfg["ngalx"], cfg["ngalz"], cfg["ny"] + 2 * cfg["dsty"] + 1],
+                       "note": "CPU FP64 restatement of the reference step (the Fortran/MPI reference does not "
+                               "build here: no Fortran compiler and FOU3D.f90 is missing)"},
+            "cpu_baseline": base,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank: int, world: int, local_rank: int, dist):
+    import littleharsh_gb300 as lh
+    cfg = WORKLOADS[args.workload]
+    prec = lh.PREC_MIXED if args.precision == "mixed" else lh.PREC_FP64
+    s, ic = build_solver(cfg, prec, seed=1 + rank)
+    pts = s.ngx * s.ngz * s.nyu
+    if args.warmup > 0:
+        s.step(args.warmup)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    import ctypes
+    rt = ctypes.CDLL("libcudart.so")
+    rt.cudaDeviceSynchronize()
+    sampler = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local_rank)).split(",")[0])
+                           if world == 1 else local_rank)
+    barrier()
+    rt.cudaDeviceSynchronize()
+    sampler.start()
+    s.step(args.steps)  # K graph launches bracketed by CUDA events on the solver's stream
+    rt.cudaDeviceSynchronize()
+    barrier()
+    clocks = sampler.stop()
+    ms, launches = s.last_step_ms()
+    ms_max = ms
+    if dist is not None:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{local_rank}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = world * pts * args.steps / (ms_max / 1e3)
+    out = None
+    if rank == 0:
+        peaks = _peaks()
+        prof = s.profile_step()
+        dom = max(prof, key=lambda k: prof[k][0])
+        dms, dn = prof[dom]
+        per_launch_ms = dms / max(dn, 1)
+        d = {"ngx": s.ngx, "ngz": s.ngz, "nkx": s.nkx, "nz": s.nz, "nyu": s.nyu, "nyv": s.nyv}
+        nl_u, nl_v = s.nyu - 2, s.nyv - 2
+        mp, npl = s.nkx * s.ngz, s.nkx * s.nz
+        csz = 16 if prec == lh.PREC_FP64 else 8
+        # compulsory bytes and model FLOPs per launch of each pipeline kernel
+        model = {
+            "zinv": ((2 * nl_u + nl_v) * (npl * 16 + mp * csz), z_flops(s.ngz, s.nkx, 2 * nl_u + nl_v)),
+            "xprod": ((2 * nl_u + nl_v + 4 * nl_u + 2 * nl_v) * mp * csz, xprod_flops(s.ngx, s.ngz, s.nkx, nl_u)),
+            "zfwd": ((4 * nl_u + 2 * nl_v) * (mp * csz + npl * 16), z_flops(s.ngz, s.nkx, 4 * nl_u + 2 * nl_v)),
+            "assemble": (19 * s.nyu * npl * 16, 0.0),
+            "vsolve": (4 * (2 * s.nyu + s.nyv) * npl * 16, 0.0),
+            "psolve": ((16 + 16 + 16 + 8 + 8) * s.nyp * npl + 14 * 16 * s.nyp * npl, 0.0),
+        }
+        bytes_l, flops_l = model.get(dom, (0, 0.0))
+        ach_gbs = bytes_l / (per_launch_ms * 1e-3) / 1e9 if bytes_l else None
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tp):
+            try:
+                traffic = json.load(open(tp)).get(f"{args.workload}:{args.precision}:{dom}")
+            except Exception:
+                traffic = None
+        roof = {"bound": "hbm", "kernel": dom, "achieved": ach_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": (ach_gbs / peaks["hbm_gbs"]) if ach_gbs else None, "traffic": traffic,
+                "peak_src": f"{peaks['src']} (MEASURED_PEAKS.json hbm_gbs)" if peaks["src"] == "measured" else "fallback",
+                "per_launch_ms": per_launch_ms, "algorithmic_bytes_per_launch": bytes_l}
+        if flops_l:
+            tf = flops_l / (per_launch_ms * 1e-3) / 1e12
+            roof["fp64"] = {"achieved": tf, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
+                            "frac": tf / peaks["fp64_tflops"], "model_flops_per_launch": flops_l,
+                            "note": "FP64 FMA peak measured on this pool (own probe)"} if prec == lh.PREC_FP64 else \
+                {"achieved": tf, "unit": "TFLOP/s (FP32 pipe)", "model_flops_per_launch": flops_l}
+        kernels = {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in prof.items()}
+        # end to end through the C ABI with host buffers: upload, one step, download
+        import torch
+        pin = [torch.empty(a.shape, dtype=torch.complex128, pin_memory=True).numpy() for a in ic]
+        s.get_fields(out=pin)
+        tinfo = s.time()
+        h2d = sum(a.nbytes for a in pin)
+        e2e_steps = max(1, min(args.steps, 3))
+        rt.cudaDeviceSynchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            s.set_fields(*pin)
+            s.set_time(tinfo["t"], tinfo["dt"], tinfo["mpgx"], tinfo["QxT"])
+            s.step(1)
+            s.get_fields(out=pin)
+        e2e_sec = (time.perf_counter() - t0) / e2e_steps
+        e2e = {"value": world * pts / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
+               "ms_per_step": e2e_sec * 1e3}
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == lh.PREC_FP64 else "mixed f32/f64",
+               "data": "synthetic (seeded laminar + 10% perturbation, projected divergence-free)",
+               "config": {"workload": args.workload, "grid_phys": [s.ngx, s.ngz, s.nyu],
+                          "modes": [2 * (s.nkx - 1), s.nz], "spectral_points": s.nkx * s.nz * s.nyu,
+                          "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (534 MB per field)",
+                          "precision": args.precision},
+               "gpu_launches": launches * args.steps, "e2e": e2e, "roofline": roof, "kernels_ms_per_step": kernels,
+               "clocks": clocks}
+        if not args.no_cpu_baseline and world == 1:
+            try:
+                out["cpu_baseline"] = cpu_baseline(cfg, os.cpu_count() or 1)
+            except Exception as e:  # reported, never fatal to the GPU number
+                out["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
+        print(json.dumps(out), flush=True)
+    s.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    else:
+        try:
+            import torch
+            torch.cuda.set_device(0)
+        except Exception:
+            pass
+    run_ours(args, rank, world, local_rank, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

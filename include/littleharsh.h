@@ -1,0 +1,207 @@
+/*
+ * littleharsh.h -- C ABI of the GB300 RK3 time step for Littleharsh.
+ *
+ * The reference advances its channel-over-canopy DNS with plain Fortran calls
+ * from the main loop (littleharsh.f90:164-190):
+ *     RHS0_u1/u2/u3, nonlinear, solveU/solveV/solveU, meanflow_ctU, solveP, v_corr
+ * on fields held in the module `declaration` (declaration.f90:133-135,
+ * type(cfield), complex(8) f(j, column)).  This header replaces that whole
+ * loop body with one call, lh_rk3_step, on device-resident fields owned by a
+ * handle.  The Fortran driver (start.f90 setup, input.in, output) keeps its
+ * role: it computes the y grid and the canopy point lists exactly as before
+ * and hands them to lh_init; a driver without a Fortran compiler can call the
+ * host helpers at the end of this header, which restate that setup.
+ *
+ * Conventions (all entry points):
+ *   - return 0 on success or a negative LH_E* code; lh_last_error(handle)
+ *     gives a one-line reason (lh_last_error(NULL) for failures before a
+ *     handle exists);
+ *   - the caller owns every host buffer; the handle owns all device memory;
+ *   - calls on one handle are not thread-safe; separate handles are
+ *     independent; each handle works on the CUDA device that was current when
+ *     lh_init ran and on the stream given in lh_params (0 = legacy default);
+ *   - complex values are interleaved (re, im) doubles, the ABI of Fortran
+ *     complex(8), C double _Complex and cuDoubleComplex.
+ *
+ * Field layouts (layout argument):
+ *   LH_LAYOUT_PLANES   [j][kk][i]: plane-major, i = 0..N1/2 fastest, then
+ *                      kk = 0..N2-1 in FFT order (kz = bet*kk for kk < N2/2,
+ *                      bet*(kk-N2) otherwise), then the y index j of the
+ *                      field's own grid.  This is the device layout.
+ *   LH_LAYOUT_COLUMNS  the reference's cfield f(j, column) for the single
+ *                      band of long columns (proc_lims_columns, start.f90:
+ *                      1092-1105, one process): j fastest, column =
+ *                      kk*(N1/2+1) + i.  The conversion is an in-HBM
+ *                      transpose on the device.
+ * Grids: u and w on the u grid j = N(4,0)..N(4,3)+1 (centres with ghosts),
+ * v on the v grid j = N(3,0)..N(3,3)+1 (faces, walls included), p on
+ * j = N(4,0)+1..N(4,3) (jlim, start.f90:1155-1174).
+ */
+#ifndef LITTLEHARSH_H
+#define LITTLEHARSH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LH_ABI_VERSION 1
+
+enum {
+  LH_OK = 0,
+  LH_EINVAL = -1,       /* bad argument, shape or parameter */
+  LH_EUNSUPPORTED = -2, /* valid for the reference but not built here (e.g. two x/z resolutions) */
+  LH_EFFT = -3,         /* a transform length does not factor into 2, 3 and 4 */
+  LH_ECUDA = -4,        /* CUDA runtime error */
+  LH_ENOMEM = -5,       /* device allocation failed */
+  LH_ESTATE = -6,       /* call out of order (e.g. step before fields or dt) */
+  LH_ENUMERIC = -7      /* non-finite value detected */
+};
+
+enum { LH_LAYOUT_PLANES = 0, LH_LAYOUT_COLUMNS = 1 };
+enum { LH_PREC_FP64 = 0, LH_PREC_MIXED = 1 };
+
+typedef struct lh_handle lh_handle;
+
+/* Everything lh_init needs besides the grid arrays.  Integer arrays follow
+ * the reference's Fortran storage: N(1:4,0:nband+1) is N[(band)*4 + row-1]. */
+typedef struct lh_params {
+  int32_t abi_version;     /* LH_ABI_VERSION */
+  int32_t N[20];           /* N(1:4,0:4)    (declaration.f90:25, set in start.f90/y_grid_canopy.f90) */
+  int32_t Ngal[20];        /* Ngal(1:4,0:4) */
+  int32_t nn;              /* nn after y_grid_canopy (= input ny - 2) */
+  int32_t flag_ctpress;    /* 0: constant flow rate (meanflow_ctU), 1: constant pressure gradient */
+  int32_t geometry_type;   /* 0 smooth, 3 canopies (only 3 has a forcing list) */
+  int32_t dsty;            /* canopy points in y, as in input.in */
+  double Re, alp, bet;
+  double ddthetavi;        /* 1/dtheta from y_grid_canopy (1 in the reference) */
+  double gridweighting[6]; /* gridweighting(1:3,1:2), Fortran order (start.f90:497-503) */
+  int32_t precision;       /* LH_PREC_FP64 or LH_PREC_MIXED */
+  int32_t reserved;
+  void* stream;            /* cudaStream_t, NULL = default stream */
+} lh_params;
+
+/* Create a solver.  Replaces the device-relevant half of `start`
+ * (start.f90:36-652): wavenumbers (def_k :655-704), RK3 coefficients
+ * (:413-427), the pressure LU (LU_buildP :628-630) and the canopy forcing
+ * lists distributed by getbounds (:706-998).
+ *   yu, dthdyu:  N(4,0)..N(4,3)+1      yv, dthdyv: N(3,0)..N(3,3)+1
+ *   dyu2i:       (3, N(4,0):N(4,3)+1)  dyv2i:      (3, N(3,0):N(3,3)+1)
+ *   list_u/list_v: (3, n) Fortran order (i, k, j), 1-based physical i,k and
+ *   global j: list_ib(:,:,ugrid) and list_ib(:,:,vgrid) of both canopies as
+ *   boundary_canopies builds them (geom_sym_canopy.f90:97-234).  Points on
+ *   planes outside the ranges getbounds hands out are dropped, as there. */
+int lh_init(const lh_params* prm, const double* yu, const double* yv, const double* dthdyu,
+            const double* dthdyv, const double* dyu2i, const double* dyv2i, const int32_t* list_u,
+            int32_t nlist_u, const int32_t* list_v, int32_t nlist_v, lh_handle** out);
+
+/* Release the handle and its device memory (part of `finalize`, littleharsh.f90:354-410). */
+void lh_free(lh_handle* h);
+
+/* Reason for the last failure on h (or of the last failed lh_init when h is NULL). */
+const char* lh_last_error(const lh_handle* h);
+
+/* Sizes: out[0..11] = nkx, nz, ngx, ngz, nyu, nyv, nyp, ju0, jv0, jp0, n_ib_planes_u, n_ib_planes_v. */
+int lh_get_sizes(const lh_handle* h, int32_t* out12);
+
+/* Upload / download u1, u2, u3, p (any may be NULL).  Uploading u1 with
+ * flag_ctpress = 0 sets the target flow rate QxT from its (0,0) column, as
+ * getini does (start.f90:1515-1518). */
+int lh_set_fields(lh_handle* h, const double* u1, const double* u2, const double* u3, const double* p,
+                  int32_t layout);
+int lh_get_fields(lh_handle* h, double* u1, double* u2, double* u3, double* p, int32_t layout);
+
+/* Nonlinear term of the previous substage (Nu1, Nu2, Nu3), same layouts. */
+int lh_set_nonlinear(lh_handle* h, const double* n1, const double* n2, const double* n3, int32_t layout);
+int lh_get_nonlinear(lh_handle* h, double* n1, double* n2, double* n3, int32_t layout);
+
+/* Scalars t, dt, mpgx; QxT < 0 keeps the current target flow rate. */
+int lh_set_time(lh_handle* h, double t, double dt, double mpgx, double QxT);
+/* out[0..4] = t, dt, mpgx, QxT, Qx (flowrateIm of the current u1). */
+int lh_get_time(lh_handle* h, double* out5);
+
+/* Advance nsteps full RK3 steps (the body of the main loop,
+ * littleharsh.f90:164-199) with the current dt.  The device work of one step
+ * is captured once into a CUDA graph and replayed. */
+int lh_rk3_step(lh_handle* h, int32_t nsteps);
+
+/* One substage kRK (1..3) up to `upto` (1 right-hand sides divided by axz,
+ * 2 after the canopy forcing, 3 after the velocity solves, 4 after the
+ * flow-rate correction, 5 complete); lh_get_rhs reads the right-hand sides. */
+int lh_substage(lh_handle* h, int32_t krk, int32_t upto);
+int lh_get_rhs(lh_handle* h, double* r1, double* r2, double* r3, int32_t layout);
+
+/* max |div u| over the p grid (error, littleharsh.f90:323-352). */
+int lh_divmax(lh_handle* h, double* out);
+/* CFL time step of the current field: cfl * min(1/max(|u|/dx+|v|/dy+|w|/dz), dtv). */
+int lh_cfl_dt(lh_handle* h, double cfl, double* dt_out);
+/* Divergence-free projection of the current velocity (solveP + v_corr with kRK = 1). */
+int lh_project(lh_handle* h);
+
+/* Spectra (spectra.f90:1-56): accumulate |u|^2, |v|^2, |w|^2, Re(u conj v_c),
+ * |p|^2 per (j, column) on the device in FP64; flush returns the sums in
+ * LH_LAYOUT_PLANES order (real, nyu/nyv/nyu/nyu/nyp planes) and the count. */
+int lh_spectra_accumulate(lh_handle* h);
+int lh_spectra_flush(lh_handle* h, double* spU, double* spV, double* spW, double* spUV, double* spP,
+                     int32_t* count, int32_t reset);
+
+/* Plane statistics (stats.f90:1-108), FP64 sums over physical planes:
+ * out is 13 x max(nyu, nyv): Um U2m Vm V2m Wm W2m Pm P2m UVm UWm VWm (rows
+ * 11-12 reserved).  Rows on the v or p grid use their first nyv / nyp entries. */
+int lh_stats_accumulate(lh_handle* h);
+int lh_stats_flush(lh_handle* h, double* out, int32_t* count, int32_t reset);
+
+/* Device time of the last lh_rk3_step call in milliseconds (CUDA events on
+ * the handle's stream) and the number of kernels one step launches. */
+int lh_last_step_ms(lh_handle* h, double* ms, int32_t* launches_per_step);
+
+/* Advance one RK3 step launch by launch (no graph) with a CUDA event after each
+ * kernel, and return the device time and launch count per kernel kind:
+ * 0 z-inverse, 1 x-pass with products, 2 z-forward, 3 right-hand-side
+ * assembly, 4/5/6 canopy forcing z-inverse / x-mask / z-forward, 7 velocity
+ * Thomas, 8 flow-rate correction, 9 pressure solve + correction.
+ * nkinds must be at least 10. */
+int lh_profile_step(lh_handle* h, double* ms_by_kind, int32_t* count_by_kind, int32_t nkinds);
+
+/* ---------------------------------------------------------------------------
+ * Host helpers restating the setup the Fortran driver does in start.f90, for
+ * drivers without a Fortran compiler.
+ * ------------------------------------------------------------------------- */
+
+/* Parsed input.in (start.f90:63-196, fixed-column FORMATs :433-436). */
+typedef struct lh_input {
+  double Re, alp, bet;
+  int32_t ngalx1, ngalx2, ngalz1, ngalz2, ny;
+  double dyq;
+  int32_t ppp, flag_init;
+  char fnameimb[96], dirin[96], dirout[96];
+  double CFL;
+  int32_t nwrite, flag_ctpress;
+  double mpgx, Kib, maxerr, maxt, maxA;
+  int32_t physlim_bot, physlim_top, geometry_type, ntilex, ntilez;
+  double posth;
+  int32_t npeakx, npeakz;
+  double Lfracx, Lfracz;
+  int32_t dsty, dstx, dstz;
+} lh_input;
+
+int lh_read_input(const char* path, lh_input* out);
+
+/* y_grid_canopy (y_grid_canopy.f90:24-194) and the band bookkeeping: fills
+ * prm (N, Ngal, nn, ddthetavi, gridweighting, Re, alp, bet, flag_ctpress,
+ * geometry_type, dsty) and the grid arrays, whose lengths are
+ * nyu = ny + 2*dsty + 1 and nyv = ny + 2*dsty. */
+int lh_setup_grid(const lh_input* in, lh_params* prm, double* yu, double* yv, double* dthdyu,
+                  double* dthdyv, double* dyu2i, double* dyv2i);
+
+/* boundary_canopies (geom_sym_canopy.f90:63-234): both canopies' lists.
+ * Call with list_u/list_v NULL to get the counts. */
+int lh_setup_canopy(const lh_input* in, const lh_params* prm, int32_t* list_u, int32_t* nlist_u,
+                    int32_t* list_v, int32_t* nlist_v);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

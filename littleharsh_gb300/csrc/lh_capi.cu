@@ -1,0 +1,980 @@
+// lh_capi.cu -- the C ABI of include/littleharsh.h.
+//
+// One handle owns one solver on one device: the read-only tables, the
+// device-resident fields and the scratch the substage pipeline needs.  A full
+// RK3 step (three substages, littleharsh.f90:164-190) is enqueued on the
+// handle's stream, captured once into a CUDA graph and replayed; nothing in the
+// step synchronises with the host.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/littleharsh.h"
+#include "lh_internal.h"
+
+using namespace lh;
+
+namespace {
+
+constexpr long double kPi = 3.141592653589793238462643383279502884L;
+thread_local std::string g_init_error;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+};
+
+// One transform length with its device tables.
+struct PlanStore {
+  FftPlan plan{};
+  DevBuf perm, tw64, tw32;
+};
+
+}  // namespace
+
+struct lh_handle {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  bool own_stream = false;
+  int precision = LH_PREC_FP64;
+  Dims d{};
+  Tables t{};
+  lh_params prm{};
+  // host copies
+  std::vector<double> yu, yv, dthdyu, dthdyv, dyu2i, dyv2i;
+  std::vector<double> kx, kz, k2x, k2z;
+  double gw[3][2]{};
+  double Re = 0, alp = 0, bet = 0, Lx = 0, Lz = 0, dtv = 0;
+  double aRK[3]{}, bRK[3]{}, gRK[3]{}, cRK[3]{}, dRK[3]{};
+  double Qx1[3]{};
+  int nibu = 0, nibv = 0;
+  int tipu[2]{-1, -1}, tipv[2]{-1, -1};
+  // device memory
+  std::vector<void*> allocs;
+  double2 *u1 = nullptr, *u2 = nullptr, *u3 = nullptr, *p = nullptr;
+  double2 *n1 = nullptr, *n2 = nullptr, *n3 = nullptr;
+  double2 *r1 = nullptr, *r2 = nullptr, *r3 = nullptr;
+  double2 *puu = nullptr, *puw = nullptr, *pww = nullptr, *pvv = nullptr, *puv = nullptr, *pvw = nullptr;
+  double2 *psi = nullptr, *lytip = nullptr, *stage = nullptr;
+  void *mixu = nullptr, *mixw = nullptr, *mixv = nullptr, *mixp[6] = {}, *mixib = nullptr, *mixly = nullptr;
+  int *ibu_lev = nullptr, *ibv_lev = nullptr, *ibu_tip = nullptr, *ibv_tip = nullptr, *ibw_tip = nullptr;
+  uint8_t *ibu_mask = nullptr, *ibv_mask = nullptr;
+  double* spec = nullptr;  // spectra accumulators
+  int nspec = 0;
+  double* tabs = nullptr;  // lu_u, lu_v, u11 (rewritten when dt changes)
+  DevScalars* sc = nullptr;
+  PlanStore pz, ph;
+  double2* rtw = nullptr;
+  int tx = 8, chunk = 16;
+  // state
+  double t_now = 0, dt = 0;
+  bool have_fields = false, have_dt = false;
+  long long iter = 0;
+  cudaGraphExec_t graph = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0;
+  int launches_per_step = 0;
+  // per-launch timing (lh_profile_step): kind of each launch and the event recorded after it
+  bool profiling = false;
+  std::vector<int> prof_kind;
+  std::vector<cudaEvent_t> prof_ev;
+  std::string err;
+};
+
+namespace {
+
+int fail(lh_handle* h, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf;
+  else g_init_error = buf;
+  return code;
+}
+
+#define CU(h, call)                                                                        \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) return fail((h), LH_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+// Kinds of launches reported by lh_profile_step.
+enum { K_ZINV, K_XPROD, K_ZFWD, K_ASSEMBLE, K_IB_ZINV, K_IB_XMASK, K_IB_ZFWD, K_VSOLVE, K_FLOWRATE, K_PSOLVE, K_NKINDS };
+
+void mark(lh_handle* h, int kind) {
+  if (!h->profiling) return;
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return;
+  cudaEventRecord(e, h->st);
+  h->prof_kind.push_back(kind);
+  h->prof_ev.push_back(e);
+}
+
+template <typename T>
+int dalloc(lh_handle* h, T** out, size_t count) {
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, count * sizeof(T) + 16);
+  if (e != cudaSuccess) return fail(h, LH_ENOMEM, "cudaMalloc(%zu bytes): %s", count * sizeof(T), cudaGetErrorString(e));
+  h->allocs.push_back(p);
+  cudaMemsetAsync(p, 0, count * sizeof(T) + 16, h->st);
+  *out = static_cast<T*>(p);
+  return LH_OK;
+}
+
+template <typename T>
+int upload(lh_handle* h, T** out, const std::vector<T>& v) {
+  int rc = dalloc(h, out, v.size());
+  if (rc) return rc;
+  CU(h, cudaMemcpyAsync(*out, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, h->st));
+  return LH_OK;
+}
+
+// Stages of a DIF sequence for length n: radix 3 first, then 2, radix 4 last
+// (the last stage needs no twiddles, which saves the most work on radix 4).
+int build_plan(lh_handle* h, PlanStore& ps, int n) {
+  FftPlan& P = ps.plan;
+  std::memset(&P, 0, sizeof P);
+  P.n = n;
+  int m = n, n4 = 0, n2 = 0, n3 = 0;
+  while (m % 4 == 0) { m /= 4; ++n4; }
+  while (m % 2 == 0) { m /= 2; ++n2; }
+  while (m % 3 == 0) { m /= 3; ++n3; }
+  if (m != 1) return fail(h, LH_EFFT, "transform length %d does not factor into 2, 3 and 4", n);
+  int s = 0;
+  for (int i = 0; i < n3; ++i) P.rad[s++] = 3;
+  for (int i = 0; i < n2; ++i) P.rad[s++] = 2;
+  for (int i = 0; i < n4; ++i) P.rad[s++] = 4;
+  if (s > kMaxStages) return fail(h, LH_EFFT, "transform length %d needs too many stages", n);
+  P.ns = s;
+  int L = n;
+  for (int i = 0; i < s; ++i) { P.len[i] = L; L /= P.rad[i]; }
+  std::vector<int> perm(n);
+  for (int f = 0; f < n; ++f) {
+    int pos = 0, x = f;
+    for (int i = 0; i < s; ++i) {
+      const int q = x % P.rad[i];
+      x /= P.rad[i];
+      pos += q * (P.len[i] / P.rad[i]);
+    }
+    perm[f] = pos;
+  }
+  std::vector<double2> t64(n);
+  std::vector<float2> t32(n);
+  for (int k = 0; k < n; ++k) {
+    const long double a = 2.0L * kPi * (long double)k / (long double)n;
+    t64[k] = double2{(double)cosl(a), -(double)sinl(a)};
+    t32[k] = float2{(float)t64[k].x, (float)t64[k].y};
+  }
+  int* dperm;
+  double2* d64;
+  float2* d32;
+  int rc;
+  if ((rc = upload(h, &dperm, perm)) || (rc = upload(h, &d64, t64)) || (rc = upload(h, &d32, t32))) return rc;
+  P.perm = dperm;
+  P.tw64 = d64;
+  P.tw32 = d32;
+  return LH_OK;
+}
+
+size_t field_elems(const lh_handle* h, char grid) {
+  const int ny = grid == 'u' ? h->d.nyu : (grid == 'v' ? h->d.nyv : h->d.nyp);
+  return (size_t)ny * h->d.np;
+}
+
+// Helmholtz LU for the three substages (LU_build + LU_dec, tridLU_3D_IB.f90:
+// 427-493,601-640) and the unit-gradient response of mode (0,0) (LUsol0,
+// :398-424) for the current dt.
+int build_dt_tables(lh_handle* h) {
+  const Dims& d = h->d;
+  const int nyu = d.nyu, nyv = d.nyv, n0 = d.nn + 3;
+  std::vector<double> all(3 * 3 * nyu + 3 * 3 * nyv + 3 * n0);
+  double* luu = all.data();
+  double* luv = luu + 9 * nyu;
+  double* u11 = luv + 9 * nyv;
+  for (int k = 0; k < 3; ++k) {
+    const double beta = h->bRK[k] * h->dt / h->Re;
+    for (int grid = 0; grid < 2; ++grid) {
+      const int ny = grid == 0 ? nyu : nyv;
+      const std::vector<double>& c = grid == 0 ? h->dyu2i : h->dyv2i;
+      double* a1 = (grid == 0 ? luu : luv) + (size_t)k * 3 * ny;
+      double* a2 = a1 + ny;
+      double* a3 = a2 + ny;
+      a1[0] = 0.0; a2[0] = 1.0; a3[0] = grid == 0 ? h->gw[1][0] : 0.0;
+      for (int j = 1; j < ny - 1; ++j) {
+        a1[j] = -beta * c[3 * j];
+        a2[j] = 1.0 - beta * (c[3 * j + 1]);
+        a3[j] = -beta * c[3 * j + 2];
+      }
+      a1[ny - 1] = grid == 0 ? h->gw[1][1] : 0.0; a2[ny - 1] = 1.0; a3[ny - 1] = 0.0;
+      a2[0] = 1.0 / a2[0];
+      for (int j = 1; j < ny; ++j) {
+        a3[j - 1] = a3[j - 1] * a2[j - 1];
+        a2[j] = 1.0 / (a2[j] - a1[j] * a3[j - 1]);
+      }
+    }
+    // LU_build0 on global indices 0..nn+2
+    const int nn = d.nn, ju0 = d.ju0;
+    std::vector<double> b1(n0), b2(n0), b3(n0);
+    b1[0] = 0.0; b2[0] = 1.0; b3[0] = h->gw[1][0];
+    for (int j = 1; j <= nn + 1; ++j) {
+      const double* c = &h->dyu2i[3 * (j - ju0)];
+      b1[j] = -beta * c[0];
+      b2[j] = 1.0 - beta * c[1];
+      b3[j] = -beta * c[2];
+    }
+    b1[nn + 2] = h->gw[1][1]; b2[nn + 2] = 1.0; b3[nn + 2] = 0.0;
+    b2[0] = 1.0 / b2[0];
+    for (int j = 1; j < n0; ++j) {
+      b3[j - 1] = b3[j - 1] * b2[j - 1];
+      b2[j] = 1.0 / (b2[j] - b1[j] * b3[j - 1]);
+    }
+    double* x = u11 + (size_t)k * n0;
+    const double bdt = -h->dRK[k] * h->dt;
+    x[0] = 0.0;
+    for (int j = 1; j <= nn + 1; ++j) x[j] = bdt;
+    x[nn + 2] = 0.0;
+    x[0] = x[0] * b2[0];
+    for (int j = 1; j < n0; ++j) x[j] = (x[j] - b1[j] * x[j - 1]) * b2[j];
+    for (int j = n0 - 2; j >= 0; --j) x[j] = x[j] - b3[j] * x[j + 1];
+    // flowrateRe sees u11(0:) as u(1:) (sequence association at littleharsh.f90:474)
+    double Q = 0.0;
+    for (int j = 1; j <= nn + 1; ++j) Q = Q + (h->yv[j - ju0] - h->yv[j - 1 - ju0]) * x[j - 1];
+    h->Qx1[k] = Q;
+  }
+  if (!h->tabs) {
+    int rc = dalloc(h, &h->tabs, all.size());
+    if (rc) return rc;
+  }
+  CU(h, cudaMemcpyAsync(h->tabs, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  h->t.lu_u = h->tabs;
+  h->t.lu_v = h->tabs + 9 * nyu;
+  h->t.u11 = h->tabs + 9 * nyu + 9 * nyv;
+  CU(h, cudaStreamSynchronize(h->st));
+  return LH_OK;
+}
+
+template <typename R>
+int enqueue_substage(lh_handle* h, int k, int upto) {
+  using T2 = cpx_t<R>;
+  const Dims& d = h->d;
+  cudaStream_t st = h->st;
+  const double beta = h->bRK[k] * h->dt / h->Re;
+  // nonlinear: z-inverse of u, w (interior centres) and v (interior faces)
+  {
+    ZJobs<R> J{};
+    J.j[0] = ZJob<R>{h->u1, nullptr, (T2*)h->mixu + d.mp, nullptr, 1, d.nyu - 2};
+    J.j[1] = ZJob<R>{h->u3, nullptr, (T2*)h->mixw + d.mp, nullptr, 1, d.nyu - 2};
+    J.j[2] = ZJob<R>{h->u2, nullptr, (T2*)h->mixv + d.mp, nullptr, 1, d.nyv - 2};
+    J.njobs = 3;
+    J.maxlev = d.nyu - 2;
+    launch_zinv<R>(J, d, h->pz.plan, h->tx, st);
+    mark(h, K_ZINV);
+  }
+  {
+    ProdArgs<R> a{};
+    a.mu = (const T2*)h->mixu;
+    a.mw = (const T2*)h->mixw;
+    a.mv = (const T2*)h->mixv;
+    for (int i = 0; i < 6; ++i) a.out[i] = (T2*)h->mixp[i];
+    a.wc = h->t.wc; a.wf = h->t.wf; a.dyc = h->t.dyc;
+    a.dxi = d.ngx / h->Lx; a.dzi = d.ngz / h->Lz;
+    a.sc = h->sc; a.want_cfl = 0; a.chunk = h->chunk;
+    launch_xprod<R>(a, d, h->ph.plan, h->rtw, st);
+    mark(h, K_XPROD);
+  }
+  {
+    ZJobs<R> J{};
+    double2* outs[6] = {h->puu, h->puw, h->pww, h->pvv, h->puv, h->pvw};
+    for (int i = 0; i < 6; ++i) {
+      const int nl = i < 4 ? d.nyu - 2 : d.nyv - 2;
+      J.j[i] = ZJob<R>{nullptr, outs[i], (T2*)h->mixp[i] + d.mp, nullptr, 1, nl};
+    }
+    J.njobs = 6;
+    J.maxlev = d.nyu - 2;
+    launch_zfwd<R>(J, d, h->pz.plan, h->tx, 1.0 / d.ngz, st);
+    mark(h, K_ZFWD);
+  }
+  {
+    AsmArgs a{};
+    a.u1 = h->u1; a.u2 = h->u2; a.u3 = h->u3; a.p = h->p;
+    a.n1 = h->n1; a.n2 = h->n2; a.n3 = h->n3;
+    a.r1 = h->r1; a.r2 = h->r2; a.r3 = h->r3;
+    a.puu = h->puu; a.puw = h->puw; a.pww = h->pww; a.pvv = h->pvv; a.puv = h->puv; a.pvw = h->pvw;
+    a.lytip = h->lytip;
+    a.tipu[0] = h->tipu[0]; a.tipu[1] = h->tipu[1]; a.tipv[0] = h->tipv[0]; a.tipv[1] = h->tipv[1];
+    a.sc = h->sc;
+    a.C1 = h->aRK[k] / h->Re; a.C2 = -h->cRK[k]; a.d = h->dRK[k]; a.g = h->gRK[k];
+    a.dt = h->dt; a.beta = beta;
+    launch_assemble(a, d, h->t, st);
+    mark(h, K_ASSEMBLE);
+  }
+  if (upto <= 1) return LH_OK;
+  if (h->nibu + h->nibv > 0) {
+    const size_t mp = d.mp;
+    T2* mib = (T2*)h->mixib;
+    ZJobs<R> J{};
+    J.j[0] = ZJob<R>{h->r1, nullptr, mib, h->ibu_lev, 0, h->nibu};
+    J.j[1] = ZJob<R>{h->r3, nullptr, mib + (size_t)h->nibu * mp, h->ibu_lev, 0, h->nibu};
+    J.j[2] = ZJob<R>{h->r2, nullptr, mib + (size_t)2 * h->nibu * mp, h->ibv_lev, 0, h->nibv};
+    J.j[3] = ZJob<R>{h->lytip, nullptr, (T2*)h->mixly, nullptr, 0, 6};
+    J.njobs = 4;
+    J.maxlev = std::max(std::max(h->nibu, h->nibv), 6);
+    launch_zinv<R>(J, d, h->pz.plan, h->tx, st);
+    mark(h, K_IB_ZINV);
+    MaskArgs<R> m{};
+    m.mix = mib;
+    m.lymix = (const T2*)h->mixly;
+    m.mask[0] = h->ibu_mask; m.mask[1] = h->ibu_mask; m.mask[2] = h->ibv_mask;
+    m.tipslot[0] = h->ibu_tip; m.tipslot[1] = h->ibw_tip; m.tipslot[2] = h->ibv_tip;
+    m.nplanes[0] = h->nibu; m.nplanes[1] = h->nibu; m.nplanes[2] = h->nibv;
+    m.beta = beta;
+    launch_xmask<R>(m, d, h->ph.plan, h->rtw, st);
+    mark(h, K_IB_XMASK);
+    ZJobs<R> F{};
+    F.j[0] = ZJob<R>{nullptr, h->r1, mib, h->ibu_lev, 0, h->nibu};
+    F.j[1] = ZJob<R>{nullptr, h->r3, mib + (size_t)h->nibu * mp, h->ibu_lev, 0, h->nibu};
+    F.j[2] = ZJob<R>{nullptr, h->r2, mib + (size_t)2 * h->nibu * mp, h->ibv_lev, 0, h->nibv};
+    F.njobs = 3;
+    F.maxlev = std::max(h->nibu, h->nibv);
+    launch_zfwd<R>(F, d, h->pz.plan, h->tx, 1.0 / d.ngz, st);
+    mark(h, K_IB_ZFWD);
+  }
+  if (upto <= 2) return LH_OK;
+  launch_vsolve(h->r1, h->r2, h->r3, h->u1, h->u2, h->u3, d, h->t, k, st);
+  mark(h, K_VSOLVE);
+  if (upto <= 3) return LH_OK;
+  if (h->prm.flag_ctpress == 0) {
+    launch_flowrate(h->u1, h->sc, d, h->t, k, h->Qx1[k], st);
+    mark(h, K_FLOWRATE);
+  }
+  if (upto <= 4) return LH_OK;
+  const double dti = 1.0 / h->dt;
+  const double dtirk = dti / (h->aRK[k] + h->bRK[k]);
+  const double dtrk = h->dt * (h->aRK[k] + h->bRK[k]);
+  launch_psolve(h->u1, h->u2, h->u3, h->p, h->psi, d, h->t, dtirk, dtrk, h->gw[0][0], h->gw[2][1], st);
+  mark(h, K_PSOLVE);
+  return LH_OK;
+}
+
+int substage(lh_handle* h, int k, int upto) {
+  int rc = h->precision == LH_PREC_MIXED ? enqueue_substage<float>(h, k, upto) : enqueue_substage<double>(h, k, upto);
+  if (rc) return rc;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(h, LH_ECUDA, "kernel launch: %s", cudaGetErrorString(e));
+  return LH_OK;
+}
+
+int count_launches(const lh_handle* h) {
+  int per = 6 + (h->prm.flag_ctpress == 0 ? 1 : 0);  // zinv, xprod, zfwd, assemble, vsolve, psolve (+flowrate)
+  if (h->nibu + h->nibv > 0) per += 3;
+  return 3 * per;
+}
+
+void free_all(lh_handle* h) {
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  for (void* p : h->allocs) cudaFree(p);
+  h->allocs.clear();
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->own_stream && h->st) cudaStreamDestroy(h->st);
+}
+
+// Host field (either layout) -> device planes
+int put_field(lh_handle* h, double2* dst, const double* src, char grid, int layout) {
+  const size_t n = field_elems(h, grid);
+  if (layout == LH_LAYOUT_PLANES) {
+    CU(h, cudaMemcpyAsync(dst, src, n * sizeof(double2), cudaMemcpyHostToDevice, h->st));
+  } else if (layout == LH_LAYOUT_COLUMNS) {
+    const int ny = (int)(n / h->d.np);
+    CU(h, cudaMemcpyAsync(h->stage, src, n * sizeof(double2), cudaMemcpyHostToDevice, h->st));
+    launch_transpose(h->stage, dst, h->d.np, ny, h->st);  // [col][j] -> [j][col]
+  } else {
+    return fail(h, LH_EINVAL, "unknown layout %d", layout);
+  }
+  CU(h, cudaStreamSynchronize(h->st));
+  return LH_OK;
+}
+
+int get_field(lh_handle* h, double* dst, const double2* src, char grid, int layout) {
+  const size_t n = field_elems(h, grid);
+  if (layout == LH_LAYOUT_PLANES) {
+    CU(h, cudaMemcpyAsync(dst, src, n * sizeof(double2), cudaMemcpyDeviceToHost, h->st));
+  } else if (layout == LH_LAYOUT_COLUMNS) {
+    const int ny = (int)(n / h->d.np);
+    launch_transpose(src, h->stage, ny, h->d.np, h->st);  // [j][col] -> [col][j]
+    CU(h, cudaMemcpyAsync(dst, h->stage, n * sizeof(double2), cudaMemcpyDeviceToHost, h->st));
+  } else {
+    return fail(h, LH_EINVAL, "unknown layout %d", layout);
+  }
+  CU(h, cudaStreamSynchronize(h->st));
+  return LH_OK;
+}
+
+int read_scalars(lh_handle* h, DevScalars* out) {
+  CU(h, cudaMemcpyAsync(out, h->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->st));
+  CU(h, cudaStreamSynchronize(h->st));
+  return LH_OK;
+}
+
+// flowrateIm of the current (0,0) column, on the host
+int host_flowrate(lh_handle* h, double* Q) {
+  const Dims& d = h->d;
+  std::vector<double2> col(d.nn + 2);
+  for (int j = 0; j <= d.nn + 1; ++j)
+    CU(h, cudaMemcpyAsync(&col[j], h->u1 + (size_t)(j - d.ju0) * d.np, sizeof(double2), cudaMemcpyDeviceToHost, h->st));
+  CU(h, cudaStreamSynchronize(h->st));
+  double q = 0.0;
+  for (int j = 1; j <= d.nn + 1; ++j) q = q + (h->yv[j - d.ju0] - h->yv[j - 1 - d.ju0]) * col[j].x;
+  *Q = q;
+  return LH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lh_last_error(const lh_handle* h) { return h ? h->err.c_str() : g_init_error.c_str(); }
+
+int lh_init(const lh_params* prm, const double* yu, const double* yv, const double* dthdyu, const double* dthdyv,
+            const double* dyu2i, const double* dyv2i, const int32_t* list_u, int32_t nlist_u, const int32_t* list_v,
+            int32_t nlist_v, lh_handle** out) {
+  if (!out) return fail(nullptr, LH_EINVAL, "out is NULL");
+  *out = nullptr;
+  if (!prm || !yu || !yv || !dthdyu || !dthdyv || !dyu2i || !dyv2i) return fail(nullptr, LH_EINVAL, "NULL argument");
+  if (prm->abi_version != LH_ABI_VERSION) return fail(nullptr, LH_EINVAL, "abi_version %d != %d", prm->abi_version, LH_ABI_VERSION);
+  auto Nf = [&](int row, int band) { return prm->N[band * 4 + row - 1]; };
+  auto Gf = [&](int row, int band) { return prm->Ngal[band * 4 + row - 1]; };
+  if (Gf(1, 1) != Gf(1, 2) || Gf(2, 1) != Gf(2, 2))
+    return fail(nullptr, LH_EUNSUPPORTED, "bands with different x/z resolutions (short columns) are not built");
+  if (prm->precision != LH_PREC_FP64 && prm->precision != LH_PREC_MIXED) return fail(nullptr, LH_EINVAL, "bad precision");
+  if (prm->geometry_type != 0 && prm->geometry_type != 3) return fail(nullptr, LH_EUNSUPPORTED, "geometry_type %d has no forcing builder", prm->geometry_type);
+  lh_handle* h = new lh_handle();
+  h->prm = *prm;
+  h->precision = prm->precision;
+  cudaGetDevice(&h->device);
+  if (prm->stream) {
+    h->st = static_cast<cudaStream_t>(prm->stream);
+  } else {
+    if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
+      delete h;
+      return fail(nullptr, LH_ECUDA, "cannot create a stream (is a CUDA device available?)");
+    }
+    h->own_stream = true;
+  }
+  auto bail = [&](int rc) {
+    g_init_error = h->err;
+    free_all(h);
+    delete h;
+    return rc;
+  };
+  Dims& d = h->d;
+  d.ngx = Gf(1, 1); d.ngz = Gf(2, 1);
+  const int nx = Nf(1, 1), nz = Nf(2, 1);
+  if (nx != 2 * (d.ngx / 3) || nz != 2 * (d.ngz / 3) || d.ngx < 6 || d.ngz < 6 || (d.ngx & 1) || (nz & 1))
+    return bail(fail(h, LH_EINVAL, "inconsistent N/Ngal"));
+  d.nkx = nx / 2 + 1;
+  d.nz = nz;
+  d.np = d.nkx * d.nz;
+  d.mp = d.nkx * d.ngz;
+  d.ju0 = Nf(4, 0);
+  if (Nf(3, 0) != d.ju0) return bail(fail(h, LH_EINVAL, "N(3,0) != N(4,0)"));
+  d.nyu = Nf(4, 3) + 1 - Nf(4, 0) + 1;
+  d.nyv = Nf(3, 3) + 1 - Nf(3, 0) + 1;
+  d.nyp = Nf(4, 3) - (Nf(4, 0) + 1) + 1;
+  d.nn = prm->nn;
+  if (d.nyv != d.nyu - 1 || d.nyp != d.nyu - 2 || d.nyu < 6) return bail(fail(h, LH_EINVAL, "inconsistent y grid sizes"));
+  if (d.nn + 2 - d.ju0 >= d.nyu || d.ju0 > 0) return bail(fail(h, LH_EINVAL, "nn outside the u grid"));
+  h->Re = prm->Re; h->alp = prm->alp; h->bet = prm->bet;
+  if (!(h->Re > 0) || !(h->alp > 0) || !(h->bet > 0)) return bail(fail(h, LH_EINVAL, "Re, alp, bet must be positive"));
+  h->Lx = 2.0 * (double)kPi / h->alp;
+  h->Lz = 2.0 * (double)kPi / h->bet;
+  for (int c = 0; c < 2; ++c)
+    for (int b = 0; b < 3; ++b) h->gw[b][c] = prm->gridweighting[c * 3 + b];
+  h->yu.assign(yu, yu + d.nyu);
+  h->yv.assign(yv, yv + d.nyv);
+  h->dthdyu.assign(dthdyu, dthdyu + d.nyu);
+  h->dthdyv.assign(dthdyv, dthdyv + d.nyv);
+  h->dyu2i.assign(dyu2i, dyu2i + 3 * d.nyu);
+  h->dyv2i.assign(dyv2i, dyv2i + 3 * d.nyv);
+  // def_k (start.f90:655-704)
+  h->kx.resize(d.nkx); h->k2x.resize(d.nkx); h->kz.resize(nz); h->k2z.resize(nz);
+  for (int i = 0; i < d.nkx; ++i) { h->kx[i] = h->alp * i; h->k2x[i] = -((h->alp * i) * (h->alp * i)); }
+  for (int k = 1; k <= nz; ++k) {
+    const double a = k <= nz / 2 ? h->bet * (k - 1) : h->bet * (nz - k + 1);
+    h->kz[k - 1] = k <= nz / 2 ? a : -a;
+    h->k2z[k - 1] = -(a * a);
+  }
+  // RK3 (start.f90:413-427)
+  const double aR[3] = {4.0 / 15.0, 1.0 / 15.0, 1.0 / 6.0}, gR[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};
+  const double cR[3] = {0.0, -17.0 / 60.0, -5.0 / 12.0}, dR[3] = {8.0 / 15.0, 2.0 / 15.0, 1.0 / 3.0};
+  for (int k = 0; k < 3; ++k) { h->aRK[k] = aR[k]; h->bRK[k] = aR[k]; h->gRK[k] = gR[k]; h->cRK[k] = cR[k]; h->dRK[k] = dR[k]; }
+  {
+    const double dyw = h->yv[1] - h->yv[0];
+    h->dtv = h->Re / (-h->k2x[nx / 2] - h->k2z[nz / 2 - 1] + 4.0 / (dyw * dyw));
+  }
+  int rc;
+  // FFT plans: z of length ngz, x through a complex transform of ngx/2
+  if ((rc = build_plan(h, h->pz, d.ngz)) || (rc = build_plan(h, h->ph, d.ngx / 2))) return bail(rc);
+  {
+    std::vector<double2> rt(d.ngx / 2 + 1);
+    for (int k = 0; k <= d.ngx / 2; ++k) {
+      const long double a = 2.0L * kPi * (long double)k / (long double)d.ngx;
+      rt[k] = double2{(double)cosl(a), -(double)sinl(a)};
+    }
+    if ((rc = upload(h, &h->rtw, rt))) return bail(rc);
+  }
+  // small tables
+  {
+    std::vector<double> cu(d.nyu), cv(d.nyv), wc(d.nyu, 0.0), wf(d.nyv, 0.0), dyc(d.nyu, 0.0), dyvw(d.nn + 2, 0.0);
+    for (int j = 0; j < d.nyu; ++j) cu[j] = prm->ddthetavi * h->dthdyu[j];
+    for (int j = 0; j < d.nyv; ++j) cv[j] = prm->ddthetavi * h->dthdyv[j];
+    for (int j = 1; j < d.nyu - 1; ++j) {
+      wc[j] = (h->yu[j] - h->yv[j - 1]) / (h->yv[j] - h->yv[j - 1]);
+      dyc[j] = 1.0 / (h->yv[j] - h->yv[j - 1]);
+    }
+    for (int j = 1; j < d.nyv - 1; ++j) wf[j] = (h->yv[j] - h->yu[j]) / (h->yu[j + 1] - h->yu[j]);
+    for (int j = 1; j <= d.nn + 1; ++j) dyvw[j] = h->yv[j - d.ju0] - h->yv[j - 1 - d.ju0];
+    double *pkx, *pkz, *pk2x, *pk2z, *pd2u, *pd2v, *pcu, *pcv, *pwc, *pwf, *pdyc, *pdyvw;
+    if ((rc = upload(h, &pkx, h->kx)) || (rc = upload(h, &pkz, h->kz)) || (rc = upload(h, &pk2x, h->k2x)) ||
+        (rc = upload(h, &pk2z, h->k2z)) || (rc = upload(h, &pd2u, h->dyu2i)) || (rc = upload(h, &pd2v, h->dyv2i)) ||
+        (rc = upload(h, &pcu, cu)) || (rc = upload(h, &pcv, cv)) || (rc = upload(h, &pwc, wc)) ||
+        (rc = upload(h, &pwf, wf)) || (rc = upload(h, &pdyc, dyc)) || (rc = upload(h, &pdyvw, dyvw)))
+      return bail(rc);
+    h->t.kx = pkx; h->t.kz = pkz; h->t.k2x = pk2x; h->t.k2z = pk2z; h->t.d2u = pd2u; h->t.d2v = pd2v;
+    h->t.cu = pcu; h->t.cv = pcv; h->t.wc = pwc; h->t.wf = pwf; h->t.dyc = pdyc; h->t.dyvw = pdyvw;
+  }
+  // pressure LU per column (LU_buildP + LU_decP)
+  {
+    const int np_ = d.nyp;
+    std::vector<double> rows(4 * (size_t)np_), dg1(np_);
+    const double dv = prm->ddthetavi;
+    for (int jp = 0; jp < np_; ++jp) {
+      const int ju = jp + 1, jvv = jp + 1;  // centre j on the u grid, face j on the v grid
+      const double Dt = dv * h->dthdyu[ju], Dbm = -dv * h->dthdyu[ju];          // D_t(j), D_b(j-1)
+      const double Gb = -dv * h->dthdyv[jvv], Gtp = dv * h->dthdyv[jvv];        // G_b(j), G_t(j+1)
+      const double Gt = jp > 0 ? dv * h->dthdyv[jvv - 1] : 0.0;                 // G_t(j) = ddthetavi*dthdyv(j-1)
+      const double Gbm = jp > 0 ? -dv * h->dthdyv[jvv - 1] : 0.0;               // G_b(j-1)
+      rows[4 * jp + 0] = Dbm * Gt;
+      rows[4 * jp + 1] = Dt * Gb;
+      rows[4 * jp + 2] = Dbm * Gbm;
+      rows[4 * jp + 3] = Dt * Gtp;
+      dg1[jp] = rows[4 * jp + 2];
+    }
+    double *prows, *pdg1, *pdg2, *pdg3;
+    if ((rc = upload(h, &prows, rows)) || (rc = upload(h, &pdg1, dg1)) ||
+        (rc = dalloc(h, &pdg2, (size_t)np_ * d.np)) || (rc = dalloc(h, &pdg3, (size_t)np_ * d.np)))
+      return bail(rc);
+    // the (0,0) Dirichlet row uses yu at global indices 1 and 2 (tridLU_3D_IB.f90:551)
+    const double dy12 = h->yu[2 - d.ju0] - h->yu[1 - d.ju0];
+    const double pin = 1.0 / (dy12 * dy12);
+    h->t.dg1 = pdg1; h->t.dg2 = pdg2; h->t.dg3 = pdg3;
+    launch_build_dg(pdg2, pdg3, prows, d, h->t, pin, h->st);
+  }
+  // canopy forcing planes and masks (getbounds filtering, start.f90:780-990)
+  {
+    const int dsty = prm->dsty;
+    const int ngal43 = Gf(4, 3), ngal33 = Gf(3, 3);
+    std::vector<int> levu, levv;
+    if (prm->geometry_type == 3) {
+      const int ulo = Nf(4, 0) + 1, uhi = Nf(4, 3), vlo = Nf(3, 0) + 1, vhi = Nf(3, 3);
+      const int ur[2][2] = {{-dsty + 1, 0}, {ngal43 - dsty + 1, ngal43}};
+      const int vr[2][2] = {{-dsty, -1}, {ngal33 + 1 - dsty + 1, ngal33 + 1}};
+      for (int c = 0; c < 2; ++c) {
+        for (int j = std::max(ur[c][0], ulo); j <= std::min(ur[c][1], uhi); ++j) levu.push_back(j - d.ju0);
+        for (int j = std::max(vr[c][0], vlo); j <= std::min(vr[c][1], vhi); ++j) levv.push_back(j - d.ju0);
+      }
+      h->tipu[0] = 0 - d.ju0; h->tipu[1] = ngal43 - dsty + 1 - d.ju0;
+      h->tipv[0] = -1 - d.ju0; h->tipv[1] = ngal33 - dsty + 2 - d.ju0;
+    }
+    h->nibu = (int)levu.size();
+    h->nibv = (int)levv.size();
+    const size_t pl = (size_t)d.ngx * d.ngz;
+    std::vector<uint8_t> mu(pl * std::max(h->nibu, 1), 0), mv(pl * std::max(h->nibv, 1), 0);
+    auto mark = [&](const int32_t* L, int n, const std::vector<int>& lev, std::vector<uint8_t>& m) -> int {
+      for (int q = 0; q < n; ++q) {
+        const int i = L[3 * q], k = L[3 * q + 1], j = L[3 * q + 2];
+        int slot = -1;
+        for (size_t s = 0; s < lev.size(); ++s)
+          if (lev[s] == j - d.ju0) { slot = (int)s; break; }
+        if (slot < 0) continue;  // outside the processed planes: dropped, as getbounds does
+        if (i < 1 || i > d.ngx || k < 1 || k > d.ngz) return -1;
+        m[(size_t)slot * pl + (size_t)(k - 1) * d.ngx + (i - 1)] = 1;
+      }
+      return 0;
+    };
+    if (h->nibu && (!list_u || nlist_u < 0)) return bail(fail(h, LH_EINVAL, "canopy list for the u grid missing"));
+    if (h->nibv && (!list_v || nlist_v < 0)) return bail(fail(h, LH_EINVAL, "canopy list for the v grid missing"));
+    if (h->nibu && mark(list_u, nlist_u, levu, mu)) return bail(fail(h, LH_EINVAL, "canopy point outside the plane"));
+    if (h->nibv && mark(list_v, nlist_v, levv, mv)) return bail(fail(h, LH_EINVAL, "canopy point outside the plane"));
+    std::vector<int> tu(std::max(h->nibu, 1), -1), tw(std::max(h->nibu, 1), -1), tv(std::max(h->nibv, 1), -1);
+    for (int s = 0; s < h->nibu; ++s) {
+      if (levu[s] == h->tipu[0]) { tu[s] = 0; tw[s] = 2; }
+      if (levu[s] == h->tipu[1]) { tu[s] = 1; tw[s] = 3; }
+    }
+    for (int s = 0; s < h->nibv; ++s) {
+      if (levv[s] == h->tipv[0]) tv[s] = 4;
+      if (levv[s] == h->tipv[1]) tv[s] = 5;
+    }
+    if (levu.empty()) levu.push_back(0);
+    if (levv.empty()) levv.push_back(0);
+    if ((rc = upload(h, &h->ibu_lev, levu)) || (rc = upload(h, &h->ibv_lev, levv)) || (rc = upload(h, &h->ibu_mask, mu)) ||
+        (rc = upload(h, &h->ibv_mask, mv)) || (rc = upload(h, &h->ibu_tip, tu)) || (rc = upload(h, &h->ibw_tip, tw)) ||
+        (rc = upload(h, &h->ibv_tip, tv)))
+      return bail(rc);
+  }
+  // fields and scratch
+  {
+    const size_t fu = field_elems(h, 'u'), fv = field_elems(h, 'v'), fp = field_elems(h, 'p');
+    if ((rc = dalloc(h, &h->u1, fu)) || (rc = dalloc(h, &h->u3, fu)) || (rc = dalloc(h, &h->u2, fv)) ||
+        (rc = dalloc(h, &h->p, fp)) || (rc = dalloc(h, &h->n1, fu)) || (rc = dalloc(h, &h->n3, fu)) ||
+        (rc = dalloc(h, &h->n2, fv)) || (rc = dalloc(h, &h->r1, fu)) || (rc = dalloc(h, &h->r3, fu)) ||
+        (rc = dalloc(h, &h->r2, fv)) || (rc = dalloc(h, &h->puu, fu)) || (rc = dalloc(h, &h->puw, fu)) ||
+        (rc = dalloc(h, &h->pww, fu)) || (rc = dalloc(h, &h->pvv, fu)) || (rc = dalloc(h, &h->puv, fv)) ||
+        (rc = dalloc(h, &h->pvw, fv)) || (rc = dalloc(h, &h->psi, fp)) || (rc = dalloc(h, &h->stage, fu)) ||
+        (rc = dalloc(h, &h->lytip, 6 * (size_t)d.np)) || (rc = dalloc(h, &h->sc, 1)))
+      return bail(rc);
+    const size_t cb = h->precision == LH_PREC_MIXED ? sizeof(float2) : sizeof(double2);
+    const size_t mu = (size_t)d.nyu * d.mp, mv = (size_t)d.nyv * d.mp;
+    unsigned char* m;
+    // mixu, mixw (u grid), mixv (v grid), then products uu, uw, ww, vv (u grid) and uv, vw (v grid)
+    if ((rc = dalloc(h, &m, cb * (6 * mu + 3 * mv)))) return bail(rc);
+    h->mixu = m; m += cb * mu;
+    h->mixw = m; m += cb * mu;
+    h->mixv = m; m += cb * mv;
+    for (int i = 0; i < 6; ++i) { h->mixp[i] = m; m += cb * (i < 4 ? mu : mv); }
+    const size_t nib = 2 * (size_t)h->nibu + h->nibv;
+    if ((rc = dalloc(h, &m, cb * (size_t)d.mp * (nib + 6)))) return bail(rc);
+    h->mixib = m;
+    h->mixly = m + cb * (size_t)d.mp * nib;
+    if ((rc = dalloc(h, &h->spec, (3 * (size_t)d.nyu + d.nyv + d.nyp) * d.np))) return bail(rc);
+  }
+  // launch shapes: z tile width and levels per x-pass chunk
+  h->tx = d.ngz * 16 * (int)sizeof(double2) <= 160 * 1024 ? 16 : 8;
+  if (h->precision == LH_PREC_MIXED && d.ngz * 32 * (int)sizeof(float2) <= 160 * 1024) h->tx = 32;
+  h->chunk = d.nyu > 256 ? 32 : 16;
+  configure_kernels();
+  if (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
+    return bail(fail(h, LH_ECUDA, "cudaEventCreate failed"));
+  {
+    DevScalars s{};
+    if (cudaMemcpyAsync(h->sc, &s, sizeof s, cudaMemcpyHostToDevice, h->st) != cudaSuccess)
+      return bail(fail(h, LH_ECUDA, "scalar upload failed"));
+  }
+  if (cudaStreamSynchronize(h->st) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+    return bail(fail(h, LH_ECUDA, "set-up kernels failed: %s", cudaGetErrorString(cudaGetLastError())));
+  h->launches_per_step = count_launches(h);
+  *out = h;
+  return LH_OK;
+}
+
+void lh_free(lh_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->st) cudaStreamSynchronize(h->st);
+  free_all(h);
+  delete h;
+}
+
+int lh_get_sizes(const lh_handle* h, int32_t* o) {
+  if (!h || !o) return LH_EINVAL;
+  const Dims& d = h->d;
+  const int v[12] = {d.nkx, d.nz, d.ngx, d.ngz, d.nyu, d.nyv, d.nyp, d.ju0, d.ju0, d.ju0 + 1, h->nibu, h->nibv};
+  std::memcpy(o, v, sizeof v);
+  return LH_OK;
+}
+
+int lh_set_fields(lh_handle* h, const double* u1, const double* u2, const double* u3, const double* p, int32_t layout) {
+  if (!h) return LH_EINVAL;
+  cudaSetDevice(h->device);
+  int rc;
+  if (u1 && (rc = put_field(h, h->u1, u1, 'u', layout))) return rc;
+  if (u2 && (rc = put_field(h, h->u2, u2, 'v', layout))) return rc;
+  if (u3 && (rc = put_field(h, h->u3, u3, 'u', layout))) return rc;
+  if (p && (rc = put_field(h, h->p, p, 'p', layout))) return rc;
+  if (u1 && h->prm.flag_ctpress != 1) {
+    double Q;
+    if ((rc = host_flowrate(h, &Q))) return rc;
+    CU(h, cudaMemcpyAsync(&h->sc->QxT, &Q, sizeof Q, cudaMemcpyHostToDevice, h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+  }
+  h->have_fields = true;
+  return LH_OK;
+}
+
+int lh_get_fields(lh_handle* h, double* u1, double* u2, double* u3, double* p, int32_t layout) {
+  if (!h) return LH_EINVAL;
+  cudaSetDevice(h->device);
+  int rc;
+  if (u1 && (rc = get_field(h, u1, h->u1, 'u', layout))) return rc;
+  if (u2 && (rc = get_field(h, u2, h->u2, 'v', layout))) return rc;
+  if (u3 && (rc = get_field(h, u3, h->u3, 'u', layout))) return rc;
+  if (p && (rc = get_field(h, p, h->p, 'p', layout))) return rc;
+  return LH_OK;
+}
+
+int lh_set_nonlinear(lh_handle* h, const double* n1, const double* n2, const double* n3, int32_t layout) {
+  if (!h) return LH_EINVAL;
+  cudaSetDevice(h->device);
+  int rc;
+  if (n1 && (rc = put_field(h, h->n1, n1, 'u', layout))) return rc;
+  if (n2 && (rc = put_field(h, h->n2, n2, 'v', layout))) return rc;
+  if (n3 && (rc = put_field(h, h->n3, n3, 'u', layout))) return rc;
+  return LH_OK;
+}
+
+int lh_get_nonlinear(lh_handle* h, double* n1, double* n2, double* n3, int32_t layout) {
+  if (!h) return LH_EINVAL;
+  cudaSetDevice(h->device);
+  int rc;
+  if (n1 && (rc = get_field(h, n1, h->n1, 'u', layout))) return rc;
+  if (n2 && (rc = get_field(h, n2, h->n2, 'v', layout))) return rc;
+  if (n3 && (rc = get_field(h, n3, h->n3, 'u', layout))) return rc;
+  return LH_OK;
+}
+
+int lh_get_rhs(lh_handle* h, double* r1, double* r2, double* r3, int32_t layout) {
+  if (!h) return LH_EINVAL;
+  cudaSetDevice(h->device);
+  int rc;
+  if (r1 && (rc = get_field(h, r1, h->r1, 'u', layout))) return rc;
+  if (r2 && (rc = get_field(h, r2, h->r2, 'v', layout))) return rc;
+  if (r3 && (rc = get_field(h, r3, h->r3, 'u', layout))) return rc;
+  return LH_OK;
+}
+
+int lh_set_time(lh_handle* h, double t, double dt, double mpgx, double QxT) {
+  if (!h) return LH_EINVAL;
+  if (!(dt > 0.0) || !std::isfinite(dt)) return fail(h, LH_EINVAL, "dt must be positive and finite");
+  cudaSetDevice(h->device);
+  h->t_now = t;
+  if (dt != h->dt || !h->have_dt) {
+    h->dt = dt;
+    h->have_dt = true;
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    int rc = build_dt_tables(h);
+    if (rc) return rc;
+  }
+  CU(h, cudaMemcpyAsync(&h->sc->mpgx, &mpgx, sizeof mpgx, cudaMemcpyHostToDevice, h->st));
+  if (QxT >= 0.0) CU(h, cudaMemcpyAsync(&h->sc->QxT, &QxT, sizeof QxT, cudaMemcpyHostToDevice, h->st));
+  CU(h, cudaStreamSynchronize(h->st));
+  return LH_OK;
+}
+
+int lh_get_time(lh_handle* h, double* o) {
+  if (!h || !o) return LH_EINVAL;
+  cudaSetDevice(h->device);
+  DevScalars s;
+  int rc = read_scalars(h, &s);
+  if (rc) return rc;
+  double Q;
+  if ((rc = host_flowrate(h, &Q))) return rc;
+  o[0] = h->t_now; o[1] = h->dt; o[2] = s.mpgx; o[3] = s.QxT; o[4] = Q;
+  return LH_OK;
+}
+
+int lh_substage(lh_handle* h, int32_t krk, int32_t upto) {
+  if (!h) return LH_EINVAL;
+  if (krk < 1 || krk > 3) return fail(h, LH_EINVAL, "kRK must be 1..3");
+  if (!h->have_fields || !h->have_dt) return fail(h, LH_ESTATE, "fields and dt must be set first");
+  cudaSetDevice(h->device);
+  int rc = substage(h, krk - 1, upto);
+  if (rc) return rc;
+  CU(h, cudaStreamSynchronize(h->st));
+  return LH_OK;
+}
+
+int lh_rk3_step(lh_handle* h, int32_t nsteps) {
+  if (!h) return LH_EINVAL;
+  if (nsteps < 0) return fail(h, LH_EINVAL, "nsteps < 0");
+  if (!h->have_fields || !h->have_dt) return fail(h, LH_ESTATE, "fields and dt must be set first");
+  cudaSetDevice(h->device);
+  if (!h->graph) {
+    cudaGraph_t g = nullptr;
+    CU(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    int rc = LH_OK;
+    for (int k = 0; k < 3 && rc == LH_OK; ++k) rc = substage(h, k, 5);
+    cudaError_t e = cudaStreamEndCapture(h->st, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return fail(h, LH_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { h->graph = nullptr; return fail(h, LH_ECUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
+  }
+  CU(h, cudaEventRecord(h->ev0, h->st));
+  for (int n = 0; n < nsteps; ++n) {
+    CU(h, cudaGraphLaunch(h->graph, h->st));
+    h->t_now += h->dt;
+    h->iter += 1;
+  }
+  CU(h, cudaEventRecord(h->ev1, h->st));
+  CU(h, cudaEventSynchronize(h->ev1));
+  float ms = 0.f;
+  CU(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+  h->last_ms = ms;
+  return LH_OK;
+}
+
+int lh_last_step_ms(lh_handle* h, double* ms, int32_t* launches) {
+  if (!h) return LH_EINVAL;
+  if (ms) *ms = h->last_ms;
+  if (launches) *launches = h->launches_per_step;
+  return LH_OK;
+}
+
+int lh_profile_step(lh_handle* h, double* ms_by_kind, int32_t* count_by_kind, int32_t nkinds) {
+  if (!h || !ms_by_kind || !count_by_kind || nkinds < K_NKINDS) return LH_EINVAL;
+  if (!h->have_fields || !h->have_dt) return fail(h, LH_ESTATE, "fields and dt must be set first");
+  cudaSetDevice(h->device);
+  CU(h, cudaStreamSynchronize(h->st));
+  cudaEvent_t e0;
+  CU(h, cudaEventCreate(&e0));
+  CU(h, cudaEventRecord(e0, h->st));
+  h->profiling = true;
+  int rc = LH_OK;
+  for (int k = 0; k < 3 && rc == LH_OK; ++k) rc = substage(h, k, 5);
+  h->profiling = false;
+  cudaError_t e = cudaStreamSynchronize(h->st);
+  for (int i = 0; i < nkinds; ++i) { ms_by_kind[i] = 0.0; count_by_kind[i] = 0; }
+  cudaEvent_t prev = e0;
+  for (size_t i = 0; i < h->prof_ev.size(); ++i) {
+    float ms = 0.f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, prev, h->prof_ev[i]);
+    ms_by_kind[h->prof_kind[i]] += ms;
+    count_by_kind[h->prof_kind[i]] += 1;
+    prev = h->prof_ev[i];
+  }
+  for (cudaEvent_t ev : h->prof_ev) cudaEventDestroy(ev);
+  h->prof_ev.clear();
+  h->prof_kind.clear();
+  cudaEventDestroy(e0);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(h, LH_ECUDA, "profiled step: %s", cudaGetErrorString(e));
+  h->t_now += h->dt;
+  h->iter += 1;
+  return LH_OK;
+}
+
+int lh_divmax(lh_handle* h, double* out) {
+  if (!h || !out) return LH_EINVAL;
+  cudaSetDevice(h->device);
+  CU(h, cudaMemsetAsync(&h->sc->cflbits, 0, sizeof(unsigned long long), h->st));
+  launch_divergence(h->u1, h->u2, h->u3, h->psi, h->d, h->t, h->st);
+  launch_absmax(h->psi, field_elems(h, 'p'), h->sc, h->st);
+  DevScalars s;
+  int rc = read_scalars(h, &s);
+  if (rc) return rc;
+  unsigned long long b = s.cflbits;
+  std::memcpy(out, &b, sizeof(double));
+  CU(h, cudaGetLastError());
+  return LH_OK;
+}
+
+int lh_cfl_dt(lh_handle* h, double cfl, double* dt_out) {
+  if (!h || !dt_out) return LH_EINVAL;
+  if (!h->have_fields) return fail(h, LH_ESTATE, "fields must be set first");
+  cudaSetDevice(h->device);
+  CU(h, cudaMemsetAsync(&h->sc->cflbits, 0, sizeof(unsigned long long), h->st));
+  const Dims& d = h->d;
+  auto run = [&](auto tag) {
+    using R = decltype(tag);
+    using T2 = cpx_t<R>;
+    ZJobs<R> J{};
+    J.j[0] = ZJob<R>{h->u1, nullptr, (T2*)h->mixu + d.mp, nullptr, 1, d.nyu - 2};
+    J.j[1] = ZJob<R>{h->u3, nullptr, (T2*)h->mixw + d.mp, nullptr, 1, d.nyu - 2};
+    J.j[2] = ZJob<R>{h->u2, nullptr, (T2*)h->mixv + d.mp, nullptr, 1, d.nyv - 2};
+    J.njobs = 3;
+    J.maxlev = d.nyu - 2;
+    launch_zinv<R>(J, d, h->pz.plan, h->tx, h->st);
+    ProdArgs<R> a{};
+    a.mu = (const T2*)h->mixu; a.mw = (const T2*)h->mixw; a.mv = (const T2*)h->mixv;
+    for (int i = 0; i < 6; ++i) a.out[i] = (T2*)h->mixp[i];
+    a.wc = h->t.wc; a.wf = h->t.wf; a.dyc = h->t.dyc;
+    a.dxi = d.ngx / h->Lx; a.dzi = d.ngz / h->Lz;
+    a.sc = h->sc; a.want_cfl = 1; a.chunk = h->chunk;
+    launch_xprod<R>(a, d, h->ph.plan, h->rtw, h->st);
+  };
+  if (h->precision == LH_PREC_MIXED) run(0.0f);
+  else run(0.0);
+  DevScalars s;
+  int rc = read_scalars(h, &s);
+  if (rc) return rc;
+  CU(h, cudaGetLastError());
+  double cmax;
+  unsigned long long b = s.cflbits;
+  std::memcpy(&cmax, &b, sizeof cmax);
+  const double dtc = cmax > 0.0 ? 1.0 / cmax : h->dtv;
+  *dt_out = cfl * (dtc < h->dtv ? dtc : h->dtv);
+  return LH_OK;
+}
+
+int lh_project(lh_handle* h) {
+  if (!h) return LH_EINVAL;
+  if (!h->have_fields) return fail(h, LH_ESTATE, "fields must be set first");
+  cudaSetDevice(h->device);
+  const double dt = h->have_dt ? h->dt : 1.0;
+  const size_t fp = field_elems(h, 'p');
+  // keep p: project with psi only
+  CU(h, cudaMemcpyAsync(h->stage, h->p, fp * sizeof(double2), cudaMemcpyDeviceToDevice, h->st));
+  const double dtirk = (1.0 / dt) / (h->aRK[0] + h->bRK[0]);
+  const double dtrk = dt * (h->aRK[0] + h->bRK[0]);
+  launch_psolve(h->u1, h->u2, h->u3, h->p, h->psi, h->d, h->t, dtirk, dtrk, h->gw[0][0], h->gw[2][1], h->st);
+  CU(h, cudaMemcpyAsync(h->p, h->stage, fp * sizeof(double2), cudaMemcpyDeviceToDevice, h->st));
+  CU(h, cudaStreamSynchronize(h->st));
+  CU(h, cudaGetLastError());
+  if (h->prm.flag_ctpress != 1) {
+    double Q;
+    int rc = host_flowrate(h, &Q);
+    if (rc) return rc;
+    CU(h, cudaMemcpyAsync(&h->sc->QxT, &Q, sizeof Q, cudaMemcpyHostToDevice, h->st));
+    CU(h, cudaStreamSynchronize(h->st));
+  }
+  return LH_OK;
+}
+
+int lh_spectra_accumulate(lh_handle* h) {
+  if (!h) return LH_EINVAL;
+  cudaSetDevice(h->device);
+  launch_spectra(h->u1, h->u2, h->u3, h->p, h->spec, h->d, h->t, h->st);
+  CU(h, cudaGetLastError());
+  h->nspec += 1;
+  return LH_OK;
+}
+
+int lh_spectra_flush(lh_handle* h, double* spU, double* spV, double* spW, double* spUV, double* spP, int32_t* count,
+                     int32_t reset) {
+  if (!h) return LH_EINVAL;
+  cudaSetDevice(h->device);
+  const size_t np = h->d.np;
+  double* b = h->spec;
+  const size_t nu = h->d.nyu * np, nv = h->d.nyv * np, npp = h->d.nyp * np;
+  double* outs[5] = {spU, spV, spW, spUV, spP};
+  const size_t lens[5] = {nu, nv, nu, nu, npp};
+  size_t off = 0;
+  for (int i = 0; i < 5; ++i) {
+    if (outs[i]) CU(h, cudaMemcpyAsync(outs[i], b + off, lens[i] * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    off += lens[i];
+  }
+  if (count) *count = h->nspec;
+  if (reset) {
+    CU(h, cudaMemsetAsync(b, 0, off * sizeof(double), h->st));
+    h->nspec = 0;
+  }
+  CU(h, cudaStreamSynchronize(h->st));
+  return LH_OK;
+}
+
+int lh_stats_accumulate(lh_handle* h) {
+  return h ? fail(h, LH_EUNSUPPORTED, "plane statistics are not built yet") : LH_EINVAL;
+}
+
+int lh_stats_flush(lh_handle* h, double*, int32_t*, int32_t) {
+  return h ? fail(h, LH_EUNSUPPORTED, "plane statistics are not built yet") : LH_EINVAL;
+}
+
+}  // extern "C"

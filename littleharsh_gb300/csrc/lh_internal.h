@@ -1,0 +1,141 @@
+// lh_internal.h -- device state and kernel launchers shared by the C ABI
+// (lh_capi.cu) and the kernels (lh_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lh_fft.cuh"
+
+namespace lh {
+
+// Geometry of the single band of long columns (every (kx,kz) column spans the
+// whole channel, as when Ngalx1 == Ngalx2 and Ngalz1 == Ngalz2).
+struct Dims {
+  int nkx, nz, ngx, ngz;   // N1/2+1, N2, Ngal1, Ngal2
+  int np;                  // spectral plane: nkx*nz complex
+  int mp;                  // mixed plane (after the z transform): nkx*ngz complex
+  int nyu, nyv, nyp;       // levels of the u, v and p grids
+  int nn;                  // reference nn (= ny-2); u11 spans 0..nn+2
+  int ju0;                 // global index of u level 0 (= jv0 = N(4,0)); p level 0 is ju0+1
+};
+
+// Read-only per-run tables in device memory.
+struct Tables {
+  const double* kx;    // [nkx] alp*i
+  const double* kz;    // [nz]  signed bet*kz
+  const double* k2x;   // [nkx] -(alp i)^2
+  const double* k2z;   // [nz]
+  const double* d2u;   // [nyu][3] dyu2i
+  const double* d2v;   // [nyv][3] dyv2i
+  const double* cu;    // [nyu] ddthetavi*dthdyu
+  const double* cv;    // [nyv] ddthetavi*dthdyv
+  const double* wc;    // [nyu] weight of face j in the centre-j interpolation of v
+  const double* wf;    // [nyv] weight of centre j+1 in the face-j interpolation of u, w
+  const double* dyc;   // [nyu] 1/(yv(j)-yv(j-1)) at centres, for the CFL number
+  const double* dyvw;  // [nn+2] yv(j)-yv(j-1), j = 1..nn+1 at index j (flow rate)
+  const double* lu_u;  // [3 kRK][3][nyu] Helmholtz LU (a1, 1/diag, scaled a3), u grid
+  const double* lu_v;  // [3 kRK][3][nyv] same, v grid
+  const double* u11;   // [3 kRK][nn+3] unit-gradient response of mode (0,0)
+  const double* dg1;   // [nyp] pressure LU lower diagonal (column independent)
+  const double* dg2;   // [nyp][np] pressure LU 1/diag per column
+  const double* dg3;   // [nyp][np] pressure LU scaled upper diagonal per column
+};
+
+// Canopy forcing: processed planes of one field.
+struct IbSet {
+  int nplanes;            // planes of the u grid (u1, u3) or v grid (u2)
+  const int* levels;      // [nplanes] level index on the field's own grid
+  const uint8_t* mask;    // [nplanes][ngz][ngx] 1 = solid
+  const int* tipslot;     // [nplanes] -1, or index of the plane's y-Laplacian in the tip buffer
+};
+
+// Scalars kept on the device so a whole step can run as one CUDA graph.
+struct DevScalars {
+  double mpgx;   // mean pressure gradient
+  double QxT;    // target flow rate
+  double Qx;     // last flow rate seen by the correction
+  unsigned long long cflbits;  // max CFL number (bit pattern of a non-negative double)
+  int err;       // sticky error flag
+};
+
+// Transform job for the z passes: nlev planes; plane y of the job reads
+// level (levels ? levels[y] : lev0 + y) of `spec` and uses mix plane y.
+template <typename R>
+struct ZJob {
+  const double2* spec_in;   // z-inverse: spectral source
+  double2* spec_out;        // z-forward: spectral destination
+  cpx_t<R>* mix;            // mixed planes, contiguous per job
+  const int* levels;
+  int lev0, nlev;
+};
+
+constexpr int kMaxJobs = 12;
+template <typename R>
+struct ZJobs {
+  ZJob<R> j[kMaxJobs];
+  int njobs, maxlev;
+};
+
+// Launchers (lh_kernels.cu).  All are asynchronous on `st`.
+template <typename R>
+void launch_zinv(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, cudaStream_t st);
+template <typename R>
+void launch_zfwd(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, double scale, cudaStream_t st);
+
+template <typename R>
+struct ProdArgs {
+  const cpx_t<R>* mu;   // [nyu] mixed planes of u (levels 1..nyu-2 used)
+  const cpx_t<R>* mw;   // [nyu] w
+  const cpx_t<R>* mv;   // [nyv] v (levels 1..nyv-2 used)
+  cpx_t<R>* out[6];     // uu, uw, ww, vv on [nyu]; uv, vw on [nyv]
+  const double* wc;
+  const double* wf;
+  const double* dyc;
+  double dxi, dzi;
+  DevScalars* sc;       // CFL maximum accumulated here when want_cfl
+  int want_cfl;
+  int chunk;
+};
+template <typename R>
+void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const double2* rtw, cudaStream_t st);
+
+template <typename R>
+struct MaskArgs {
+  cpx_t<R>* mix;          // all processed planes, contiguous: [nplanes_total][ngz][nkx]
+  const cpx_t<R>* lymix;  // tip planes' y-Laplacian
+  const uint8_t* mask[3];
+  const int* tipslot[3];
+  int nplanes[3];
+  double beta;
+};
+template <typename R>
+void launch_xmask(const MaskArgs<R>& a, const Dims& d, const FftPlan& ph, const double2* rtw, cudaStream_t st);
+
+struct AsmArgs {
+  const double2 *u1, *u2, *u3, *p;
+  double2 *n1, *n2, *n3;     // in: Nu of the previous substage, out: Nu of this one
+  double2 *r1, *r2, *r3;     // out: right-hand sides divided by axz
+  const double2 *puu, *puw, *pww, *pvv, *puv, *pvw;
+  double2* lytip;            // y-Laplacian of the tip planes [6][np]
+  int tipu[2], tipv[2];      // level indices of the tip planes (u grid, v grid) or -1
+  const DevScalars* sc;
+  double C1, C2, d, g, dt, beta;
+};
+void launch_assemble(const AsmArgs& a, const Dims& d, const Tables& t, cudaStream_t st);
+
+void launch_vsolve(double2* r1, double2* r2, double2* r3, double2* u1, double2* u2, double2* u3,
+                   const Dims& d, const Tables& t, int k, cudaStream_t st);
+void launch_flowrate(double2* u1, DevScalars* sc, const Dims& d, const Tables& t, int k, double Qx1, cudaStream_t st);
+void launch_build_dg(double* dg2, double* dg3, const double* rows, const Dims& d, const Tables& t, double pin,
+                     cudaStream_t st);
+void launch_psolve(double2* u1, double2* u2, double2* u3, double2* p, double2* psi, const Dims& d,
+                   const Tables& t, double dtirk, double dtrk, double gwb, double gwt, cudaStream_t st);
+void launch_divergence(const double2* u1, const double2* u2, const double2* u3, double2* div, const Dims& d,
+                       const Tables& t, cudaStream_t st);
+void launch_absmax(const double2* x, size_t n, DevScalars* sc, cudaStream_t st);
+void launch_transpose(const double2* src, double2* dst, int rows, int cols, cudaStream_t st);
+void launch_spectra(const double2* u1, const double2* u2, const double2* u3, const double2* p, double* sp,
+                    const Dims& d, const Tables& t, cudaStream_t st);
+void configure_kernels();
+
+}  // namespace lh

@@ -1,0 +1,784 @@
+// lh_kernels.cu -- sm_103a kernels of the Littleharsh RK3 substage.
+//
+// Data layout in HBM: every spectral field is plane-major complex
+// [level][kk][i] (i = kx index fastest).  The reference moves y-pencils of one
+// (kx,kz) column to x-z planes with MPI all-to-alls (FOU3D.f90, missing from
+// the tree; call sites littleharsh.f90:171, tridLU_3D_IB.f90:220-245,302-324);
+// here a plane kernel reads planes directly and a column kernel walks the
+// levels of one column with coalesced per-level accesses, so no transpose
+// pass exists in the step.
+//
+// Per substage:
+//   zinv   z-inverse of u, w, v with 3/2 zero padding (the dk shift,
+//          start.f90:1177-1205)                          -> mixed planes
+//   xprod  x-inverse, y-interpolation to the other grid, the six products,
+//          x-forward with truncation                      -> mixed products
+//   zfwd   z-forward with truncation                      -> product spectra
+//   assemble  RHS0_u1/2/3 (littleharsh.f90:614-731) + the reconstructed
+//          nonlinear term + solveU/V's u+dt*du and the axz division
+//          (tridLU_3D_IB.f90:90-98)
+//   zinv/xmask/zfwd  canopy forcing on the processed planes
+//          (immersed_boundaries_U/V, tridLU_3D_IB.f90:198-359)
+//   vsolve Thomas sweeps with the shared y LU (tridLU_3D_IB.f90:106-116,179-189)
+//   flowrate  meanflow_ctU/flowrate_corr on mode (0,0) (littleharsh.f90:453-485)
+//   psolve divergence, pressure LU per column, p += psi, v_corr
+//          (littleharsh.f90:557-612,826-937; tridLU_3D_IB.f90:362-396)
+#include <cstdio>
+
+#include "lh_internal.h"
+
+namespace lh {
+
+// ---------------------------------------------------------------------------
+// z passes
+// ---------------------------------------------------------------------------
+
+// Batch-fast DIF: consecutive threads take consecutive vectors of the batch,
+// so a warp touches contiguous shared memory when vectors are interleaved.
+template <typename R, int SIGN>
+__device__ void fft_dif_bfast(cpx_t<R>* buf, int nb, int es, const FftPlan& P) {
+  using T2 = cpx_t<R>;
+  const T2* __restrict__ tw = twtab<R>(P);
+  const int n = P.n;
+  for (int s = 0; s < P.ns; ++s) {
+    const int r = P.rad[s], L = P.len[s], m = L / r, ts = n / L;
+    const int nbf = n / r;
+    const int total = nb * nbf;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+      const int f = t / nb, b = t - f * nb;
+      const int blk = f / m, k = f - blk * m;
+      T2* base = buf + b + (blk * L + k) * es;
+      const int st = m * es;
+      if (r == 4) {
+        T2 a = base[0], bb = base[st], c = base[2 * st], d = base[3 * st];
+        T2 t0 = cadd(a, c), t1 = csub(a, c), t2 = cadd(bb, d), t3 = csub(bb, d);
+        T2 u = (SIGN < 0) ? T2{t3.y, -t3.x} : T2{-t3.y, t3.x};
+        T2 y0 = cadd(t0, t2), y2 = csub(t0, t2), y1 = cadd(t1, u), y3 = csub(t1, u);
+        if (m > 1) {
+          y1 = ctw<SIGN>(y1, tw[k * ts]);
+          y2 = ctw<SIGN>(y2, tw[2 * k * ts]);
+          y3 = ctw<SIGN>(y3, tw[3 * k * ts]);
+        }
+        base[0] = y0; base[st] = y1; base[2 * st] = y2; base[3 * st] = y3;
+      } else if (r == 2) {
+        T2 a = base[0], bb = base[st];
+        T2 y0 = cadd(a, bb), y1 = csub(a, bb);
+        if (m > 1) y1 = ctw<SIGN>(y1, tw[k * ts]);
+        base[0] = y0; base[st] = y1;
+      } else {
+        const R h = (R)0.5;
+        const R s3 = (SIGN < 0) ? (R)-0.86602540378443864676 : (R)0.86602540378443864676;
+        T2 a = base[0], bb = base[st], c = base[2 * st];
+        T2 t1 = cadd(bb, c), d = csub(bb, c);
+        T2 t2 = T2{a.x - h * t1.x, a.y - h * t1.y};
+        T2 u = T2{-s3 * d.y, s3 * d.x};
+        T2 y0 = cadd(a, t1), y1 = cadd(t2, u), y2 = csub(t2, u);
+        if (m > 1) {
+          y1 = ctw<SIGN>(y1, tw[k * ts]);
+          y2 = ctw<SIGN>(y2, tw[2 * k * ts]);
+        }
+        base[0] = y0; base[st] = y1; base[2 * st] = y2;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_zinv(ZJobs<R> jobs, Dims d, FftPlan pz, int tx) {
+  using T2 = cpx_t<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T2* sm = reinterpret_cast<T2*>(smraw);  // [ngz][tx]
+  const int job = blockIdx.z;
+  const ZJob<R> J = jobs.j[job];
+  const int y = blockIdx.y;
+  if (y >= J.nlev) return;
+  const int lev = J.levels ? J.levels[y] : J.lev0 + y;
+  const int i0 = blockIdx.x * tx;
+  const int nb = min(tx, d.nkx - i0);
+  const double2* __restrict__ src = J.spec_in + (size_t)lev * d.np;
+  const int h = d.nz / 2, gap = d.ngz - d.nz;
+  for (int e = threadIdx.x; e < gap * tx; e += blockDim.x) sm[(h + e / tx) * tx + (e % tx)] = T2{0, 0};
+  for (int e = threadIdx.x; e < d.nz * tx; e += blockDim.x) {
+    const int kk = e / tx, c = e - kk * tx;
+    const int slot = kk < h ? kk : kk + gap;
+    T2 v = T2{0, 0};
+    if (c < nb) {
+      const double2 s = src[(size_t)kk * d.nkx + i0 + c];
+      v = T2{(R)s.x, (R)s.y};
+    }
+    sm[slot * tx + c] = v;
+  }
+  __syncthreads();
+  fft_dif_bfast<R, +1>(sm, nb, tx, pz);
+  T2* __restrict__ dst = J.mix + (size_t)y * d.mp;
+  for (int e = threadIdx.x; e < d.ngz * tx; e += blockDim.x) {
+    const int z = e / tx, c = e - z * tx;
+    if (c < nb) dst[(size_t)z * d.nkx + i0 + c] = sm[pz.perm[z] * tx + c];
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_zfwd(ZJobs<R> jobs, Dims d, FftPlan pz, int tx, double scale) {
+  using T2 = cpx_t<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T2* sm = reinterpret_cast<T2*>(smraw);  // [ngz][tx]
+  const int job = blockIdx.z;
+  const ZJob<R> J = jobs.j[job];
+  const int y = blockIdx.y;
+  if (y >= J.nlev) return;
+  const int lev = J.levels ? J.levels[y] : J.lev0 + y;
+  const int i0 = blockIdx.x * tx;
+  const int nb = min(tx, d.nkx - i0);
+  const T2* __restrict__ src = J.mix + (size_t)y * d.mp;
+  for (int e = threadIdx.x; e < d.ngz * tx; e += blockDim.x) {
+    const int z = e / tx, c = e - z * tx;
+    sm[z * tx + c] = (c < nb) ? src[(size_t)z * d.nkx + i0 + c] : T2{0, 0};
+  }
+  __syncthreads();
+  fft_dif_bfast<R, -1>(sm, nb, tx, pz);
+  double2* __restrict__ dst = J.spec_out + (size_t)lev * d.np;
+  const int h = d.nz / 2, gap = d.ngz - d.nz;
+  for (int e = threadIdx.x; e < d.nz * tx; e += blockDim.x) {
+    const int kk = e / tx, c = e - kk * tx;
+    if (c < nb) {
+      const int slot = kk < h ? kk : kk + gap;
+      const T2 v = sm[pz.perm[slot] * tx + c];
+      dst[(size_t)kk * d.nkx + i0 + c] = double2{(double)v.x * scale, (double)v.y * scale};
+    }
+  }
+}
+
+template <typename R>
+void launch_zinv(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, cudaStream_t st) {
+  if (jobs.njobs == 0 || jobs.maxlev == 0) return;
+  dim3 grid((d.nkx + tx - 1) / tx, jobs.maxlev, jobs.njobs);
+  size_t sm = sizeof(cpx_t<R>) * (size_t)d.ngz * tx;
+  k_zinv<R><<<grid, 256, sm, st>>>(jobs, d, pz, tx);
+}
+
+template <typename R>
+void launch_zfwd(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, double scale, cudaStream_t st) {
+  if (jobs.njobs == 0 || jobs.maxlev == 0) return;
+  dim3 grid((d.nkx + tx - 1) / tx, jobs.maxlev, jobs.njobs);
+  size_t sm = sizeof(cpx_t<R>) * (size_t)d.ngz * tx;
+  k_zfwd<R><<<grid, 256, sm, st>>>(jobs, d, pz, tx, scale);
+}
+
+// ---------------------------------------------------------------------------
+// x passes: real transforms of length ngx through complex DIFs of length h = ngx/2
+// ---------------------------------------------------------------------------
+
+// Inverse real transform of `nr` mixed rows (nkx complex each, zero beyond)
+// into physical rows (ngx reals).  F: nr vectors of hp complex.
+template <typename R>
+__device__ void x_inverse(const cpx_t<R>* const* rows, int nr, cpx_t<R>* F, int hp, R* const* out, const Dims& d,
+                          const FftPlan& ph, const double2* __restrict__ rtw) {
+  using T2 = cpx_t<R>;
+  const int h = d.ngx / 2, nkx = d.nkx;
+  for (int e = threadIdx.x; e < nr * h; e += blockDim.x) {
+    const int r = e / h, k = e - r * h;
+    const T2* row = rows[r];
+    T2 a = (k < nkx) ? row[k] : T2{0, 0};
+    if (k == 0) a.y = 0;
+    const int k2 = h - k;  // k = 0 pairs with X[h] = 0
+    T2 b = (k > 0 && k2 < nkx) ? row[k2] : T2{0, 0};
+    b.y = -b.y;
+    const T2 s = cadd(a, b), df = csub(a, b);
+    const double2 w = rtw[k];
+    const R wr = (R)w.x, wi = (R)-w.y;  // exp(+2 pi i k/n)
+    const T2 q = T2{wr * df.x - wi * df.y, wr * df.y + wi * df.x};
+    F[r * hp + k] = T2{s.x - q.y, s.y + q.x};
+  }
+  __syncthreads();
+  fft_dif<R, +1>(F, nr, 1, hp, ph);
+  for (int e = threadIdx.x; e < nr * h; e += blockDim.x) {
+    const int r = e / h, m = e - r * h;
+    const T2 z = F[r * hp + ph.perm[m]];
+    out[r][2 * m] = z.x;
+    out[r][2 * m + 1] = z.y;
+  }
+  __syncthreads();
+}
+
+// Forward real transform of the data already packed in F (z[m] = x[2m] + i
+// x[2m+1], natural order) into nr mixed rows scaled by 1/ngx, kx < nkx kept.
+template <typename R>
+__device__ void x_forward_packed(int nr, cpx_t<R>* F, int hp, cpx_t<R>* const* rows, const Dims& d,
+                                 const FftPlan& ph, const double2* __restrict__ rtw) {
+  using T2 = cpx_t<R>;
+  const int h = d.ngx / 2, nkx = d.nkx;
+  const R scale = (R)(1.0 / d.ngx);
+  fft_dif<R, -1>(F, nr, 1, hp, ph);
+  for (int e = threadIdx.x; e < nr * nkx; e += blockDim.x) {
+    const int r = e / nkx, k = e - r * nkx;
+    const T2 zk = F[r * hp + ph.perm[k]];
+    const int k2 = (h - k) % h;
+    T2 zc = F[r * hp + ph.perm[k2]];
+    zc.y = -zc.y;
+    const T2 E = T2{(R)0.5 * (zk.x + zc.x), (R)0.5 * (zk.y + zc.y)};
+    const T2 D = csub(zk, zc);
+    const T2 O = T2{(R)0.5 * D.y, (R)-0.5 * D.x};
+    const double2 w = rtw[k];
+    const R wr = (R)w.x, wi = (R)w.y;
+    T2 X = T2{E.x + (wr * O.x - wi * O.y), E.y + (wr * O.y + wi * O.x)};
+    X.x = scale * X.x;
+    X.y = (k == 0) ? (R)0 : scale * X.y;
+    rows[r][k] = X;
+  }
+  __syncthreads();
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph, const double2* __restrict__ rtw) {
+  using T2 = cpx_t<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int ngx = d.ngx, h = ngx / 2, hp = h + 1;
+  T2* F = reinterpret_cast<T2*>(smraw);       // 6 vectors of hp
+  R* rowsm = reinterpret_cast<R*>(F + 6 * hp);  // 6 rows of ngx
+  R* up = rowsm;
+  R* wp = rowsm + ngx;
+  R* vp = rowsm + 2 * ngx;
+  R* uc = rowsm + 3 * ngx;
+  R* wc = rowsm + 4 * ngx;
+  R* vc = rowsm + 5 * ngx;
+  __shared__ double cflred[8];
+  const int kz = blockIdx.x;
+  const int c0 = 1 + blockIdx.y * a.chunk;
+  const int c1 = min(c0 + a.chunk - 1, d.nyu - 2);
+  if (c0 > c1) return;
+  const size_t rowoff = (size_t)kz * d.nkx;
+  double cmax = 0.0;
+  // warm-up: previous centre and face
+  if (c0 - 1 >= 1) {
+    const T2* rows[3] = {a.mu + (size_t)(c0 - 1) * d.mp + rowoff, a.mw + (size_t)(c0 - 1) * d.mp + rowoff,
+                         a.mv + (size_t)(c0 - 1) * d.mp + rowoff};
+    R* outs[3] = {up, wp, vp};
+    x_inverse<R>(rows, 3, F, hp, outs, d, ph, rtw);
+  } else {
+    for (int x = threadIdx.x; x < 3 * ngx; x += blockDim.x) up[x] = (R)0;
+    __syncthreads();
+  }
+  for (int jj = c0; jj <= c1; ++jj) {
+    const bool vface = jj <= d.nyv - 2;  // face jj interior (else the top wall, v = 0)
+    {
+      const T2* rows[3] = {a.mu + (size_t)jj * d.mp + rowoff, a.mw + (size_t)jj * d.mp + rowoff,
+                           a.mv + (size_t)jj * d.mp + rowoff};
+      R* outs[3] = {uc, wc, vc};
+      if (!vface)
+        for (int x = threadIdx.x; x < ngx; x += blockDim.x) vc[x] = (R)0;
+      x_inverse<R>(rows, vface ? 3 : 2, F, hp, outs, d, ph, rtw);
+    }
+    const bool fprod = jj - 1 >= 1;  // face jj-1 interior
+    const R wcj = (R)a.wc[jj];
+    const R wfj = fprod ? (R)a.wf[jj - 1] : (R)0;
+    const double dyi = a.dyc[jj];
+    for (int m = threadIdx.x; m < h; m += blockDim.x) {
+      R q[6][2];
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int x = 2 * m + e;
+        const R u = uc[x], w = wc[x];
+        const R v = vp[x] + wcj * (vc[x] - vp[x]);
+        q[0][e] = u * u;
+        q[1][e] = u * w;
+        q[2][e] = w * w;
+        q[3][e] = v * v;
+        if (fprod) {
+          const R uf = up[x] + wfj * (u - up[x]);
+          const R wf = wp[x] + wfj * (w - wp[x]);
+          q[4][e] = uf * vp[x];
+          q[5][e] = wf * vp[x];
+        }
+        if (a.want_cfl) {
+          const double cv = fabs((double)u) * a.dxi + fabs((double)v) * dyi + fabs((double)w) * a.dzi;
+          cmax = fmax(cmax, cv);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+        if (r < 4 || fprod) F[r * hp + m] = T2{q[r][0], q[r][1]};
+    }
+    __syncthreads();
+    {
+      T2* rows[6] = {a.out[0] + (size_t)jj * d.mp + rowoff, a.out[1] + (size_t)jj * d.mp + rowoff,
+                     a.out[2] + (size_t)jj * d.mp + rowoff, a.out[3] + (size_t)jj * d.mp + rowoff,
+                     a.out[4] + (size_t)(jj - 1) * d.mp + rowoff, a.out[5] + (size_t)(jj - 1) * d.mp + rowoff};
+      x_forward_packed<R>(fprod ? 6 : 4, F, hp, rows, d, ph, rtw);
+    }
+    // current becomes previous
+    R* t;
+    t = up; up = uc; uc = t;
+    t = wp; wp = wc; wc = t;
+    t = vp; vp = vc; vc = t;
+  }
+  if (a.want_cfl) {
+    for (int o = 16; o > 0; o >>= 1) cmax = fmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, o));
+    if ((threadIdx.x & 31) == 0) cflred[threadIdx.x >> 5] = cmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double m = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, cflred[w]);
+      atomicMax(&a.sc->cflbits, (unsigned long long)__double_as_longlong(m));
+    }
+  }
+}
+
+template <typename R>
+void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const double2* rtw, cudaStream_t st) {
+  const int ncent = d.nyu - 2;
+  if (ncent <= 0) return;
+  dim3 grid(d.ngz, (ncent + a.chunk - 1) / a.chunk);
+  const int hp = d.ngx / 2 + 1;
+  size_t sm = sizeof(cpx_t<R>) * 6 * (size_t)hp + sizeof(R) * 6 * (size_t)d.ngx;
+  k_xprod<R><<<grid, 256, sm, st>>>(a, d, ph, rtw);
+}
+
+// Canopy forcing on one mixed row of one processed plane: x-inverse, solid
+// points set to 0 (or -beta*Luy on the tip planes), x-forward.
+template <typename R>
+__global__ void __launch_bounds__(128) k_xmask(MaskArgs<R> a, Dims d, FftPlan ph, const double2* __restrict__ rtw) {
+  using T2 = cpx_t<R>;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int ngx = d.ngx, h = ngx / 2, hp = h + 1;
+  T2* F = reinterpret_cast<T2*>(smraw);
+  R* rr = reinterpret_cast<R*>(F + 2 * hp);
+  R* ll = rr + ngx;
+  const int kz = blockIdx.x;
+  int pl = blockIdx.y, f = 0;
+  while (f < 2 && pl >= a.nplanes[f]) { pl -= a.nplanes[f]; ++f; }
+  size_t plane = (size_t)blockIdx.y;
+  T2* row = a.mix + plane * d.mp + (size_t)kz * d.nkx;
+  const int tip = a.tipslot[f][pl];
+  {
+    const T2* rows[2] = {row, tip >= 0 ? a.lymix + (size_t)tip * d.mp + (size_t)kz * d.nkx : row};
+    R* outs[2] = {rr, ll};
+    x_inverse<R>(rows, tip >= 0 ? 2 : 1, F, hp, outs, d, ph, rtw);
+  }
+  const uint8_t* msk = a.mask[f] + ((size_t)pl * d.ngz + kz) * ngx;
+  const R mb = (R)(-a.beta);
+  for (int m = threadIdx.x; m < h; m += blockDim.x) {
+    R v[2];
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int x = 2 * m + e;
+      v[e] = rr[x];
+      if (msk[x]) v[e] = (tip >= 0) ? mb * ll[x] : (R)0;
+    }
+    F[m] = T2{v[0], v[1]};
+  }
+  __syncthreads();
+  T2* rows[1] = {row};
+  x_forward_packed<R>(1, F, hp, rows, d, ph, rtw);
+}
+
+template <typename R>
+void launch_xmask(const MaskArgs<R>& a, const Dims& d, const FftPlan& ph, const double2* rtw, cudaStream_t st) {
+  const int tot = a.nplanes[0] + a.nplanes[1] + a.nplanes[2];
+  if (tot == 0) return;
+  dim3 grid(d.ngz, tot);
+  const int hp = d.ngx / 2 + 1;
+  size_t sm = sizeof(cpx_t<R>) * 2 * (size_t)hp + sizeof(R) * 2 * (size_t)d.ngx;
+  k_xmask<R><<<grid, 128, sm, st>>>(a, d, ph, rtw);
+}
+
+// ---------------------------------------------------------------------------
+// column-local kernels (always FP64)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ double2 ld(const double2* p) { return __ldg(p); }
+
+__global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= d.np) return;
+  const int jj = blockIdx.y;
+  const int np = d.np;
+  const int i = col % d.nkx, kk = col / d.nkx;
+  const double kx = t.kx[i], kz = t.kz[kk], k2 = t.k2x[i] + t.k2z[kk];
+  const double axz = 1.0 - a.beta * (t.k2x[i] + t.k2z[kk]);
+  const size_t c0 = (size_t)jj * np + col;
+  // u1 and u3 on centre jj
+  if (jj == 0 || jj == d.nyu - 1) {
+    a.r1[c0] = double2{0.0, 0.0};
+    a.r3[c0] = double2{0.0, 0.0};
+  } else {
+    const double a1 = t.d2u[3 * jj], a2 = t.d2u[3 * jj + 1], a3 = t.d2u[3 * jj + 2];
+    const double2 pc = ld(a.p + (size_t)(jj - 1) * np + col);
+    const double c = t.cu[jj];
+    const size_t f1 = (size_t)jj * np + col, f0 = f1 - np;  // faces jj and jj-1
+    const bool tip = (jj == a.tipu[0] || jj == a.tipu[1]);
+    const int tslot = (jj == a.tipu[0]) ? 0 : 1;
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
+      const double2* u = f == 0 ? a.u1 : a.u3;
+      const double2 um = ld(u + c0 - np), u0 = ld(u + c0), up = ld(u + c0 + np);
+      const double L_x = a1 * um.x + (k2 + a2) * u0.x + a3 * up.x;
+      const double L_y = a1 * um.y + (k2 + a2) * u0.y + a3 * up.y;
+      const double kf = f == 0 ? kx : kz;
+      const double2 nold = (f == 0 ? a.n1 : a.n3)[c0];
+      double rx = a.C1 * L_x + a.C2 * nold.x + (a.d * kf) * pc.y;
+      double ry = a.C1 * L_y + a.C2 * nold.y + -(a.d * kf) * pc.x;
+      if (f == 0 && col == 0) rx = rx + (-a.d * a.sc->mpgx);
+      const double2 A = ld((f == 0 ? a.puu : a.puw) + c0);
+      const double2 B = ld((f == 0 ? a.puw : a.pww) + c0);
+      const double2* D = f == 0 ? a.puv : a.pvw;
+      const double2 D1 = ld(D + f1), D0 = ld(D + f0);
+      const double nr = (-kx * A.y - kz * B.y) + c * (D1.x - D0.x);
+      const double ni = (kx * A.x + kz * B.x) + c * (D1.y - D0.y);
+      (f == 0 ? a.n1 : a.n3)[c0] = double2{nr, ni};
+      rx = rx - a.g * nr;
+      ry = ry - a.g * ni;
+      (f == 0 ? a.r1 : a.r3)[c0] = double2{(u0.x + a.dt * rx) / axz, (u0.y + a.dt * ry) / axz};
+      if (tip) {
+        const double ly_x = a1 * um.x + (a2)*u0.x + a3 * up.x;
+        const double ly_y = a1 * um.y + (a2)*u0.y + a3 * up.y;
+        a.lytip[(size_t)(2 * f + tslot) * np + col] = double2{ly_x, ly_y};
+      }
+    }
+  }
+  // u2 on face jj
+  if (jj <= d.nyv - 1) {
+    if (jj == 0 || jj == d.nyv - 1) {
+      a.r2[c0] = double2{0.0, 0.0};
+    } else {
+      const double a1 = t.d2v[3 * jj], a2 = t.d2v[3 * jj + 1], a3 = t.d2v[3 * jj + 2];
+      const double2 um = ld(a.u2 + c0 - np), u0 = ld(a.u2 + c0), up = ld(a.u2 + c0 + np);
+      const double2 p0 = ld(a.p + (size_t)(jj - 1) * np + col), p1 = ld(a.p + (size_t)jj * np + col);
+      const double C3 = -a.d * t.cv[jj];
+      const double L_x = a1 * um.x + (k2 + a2) * u0.x + a3 * up.x;
+      const double L_y = a1 * um.y + (k2 + a2) * u0.y + a3 * up.y;
+      const double2 nold = a.n2[c0];
+      double rx = a.C1 * L_x + a.C2 * nold.x + C3 * (p1.x - p0.x);
+      double ry = a.C1 * L_y + a.C2 * nold.y + C3 * (p1.y - p0.y);
+      const double2 A = ld(a.puv + c0), B = ld(a.pvw + c0);
+      const double2 V1 = ld(a.pvv + c0 + np), V0 = ld(a.pvv + c0);
+      const double c = t.cv[jj];
+      const double nr = (-kx * A.y - kz * B.y) + c * (V1.x - V0.x);
+      const double ni = (kx * A.x + kz * B.x) + c * (V1.y - V0.y);
+      a.n2[c0] = double2{nr, ni};
+      rx = rx - a.g * nr;
+      ry = ry - a.g * ni;
+      a.r2[c0] = double2{(u0.x + a.dt * rx) / axz, (u0.y + a.dt * ry) / axz};
+      if (jj == a.tipv[0] || jj == a.tipv[1]) {
+        const int tslot = (jj == a.tipv[0]) ? 0 : 1;
+        a.lytip[(size_t)(4 + tslot) * np + col] =
+            double2{a1 * um.x + (a2)*u0.x + a3 * up.x, a1 * um.y + (a2)*u0.y + a3 * up.y};
+      }
+    }
+  }
+}
+
+void launch_assemble(const AsmArgs& a, const Dims& d, const Tables& t, cudaStream_t st) {
+  dim3 grid((d.np + 255) / 256, d.nyu);
+  k_assemble<<<grid, 256, 0, st>>>(a, d, t);
+}
+
+// Thomas sweeps with the band's shared LU (LUsolU/LUsolV).  One thread per
+// (component, column); levels are prefetched four at a time.
+__global__ void __launch_bounds__(128) k_vsolve(double2* r1, double2* r2, double2* r3, double2* u1, double2* u2,
+                                                double2* u3, Dims d, Tables t, int k) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= d.np) return;
+  const int comp = blockIdx.y;
+  const int ny = comp == 1 ? d.nyv : d.nyu;
+  const double* lu = comp == 1 ? t.lu_v + (size_t)k * 3 * d.nyv : t.lu_u + (size_t)k * 3 * d.nyu;
+  const double* a1 = lu;
+  const double* a2 = lu + ny;
+  const double* a3 = lu + 2 * ny;
+  double2* R = comp == 0 ? r1 : (comp == 1 ? r2 : r3);
+  double2* U = comp == 0 ? u1 : (comp == 1 ? u2 : u3);
+  const size_t np = d.np;
+  double2 x = R[col];
+  x = double2{x.x * a2[0], x.y * a2[0]};
+  R[col] = x;
+  int jj = 1;
+  for (; jj + 3 < ny; jj += 4) {
+    double2 v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = R[(size_t)(jj + q) * np + col];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const double b1 = a1[jj + q], b2 = a2[jj + q];
+      x = double2{(v[q].x - b1 * x.x) * b2, (v[q].y - b1 * x.y) * b2};
+      R[(size_t)(jj + q) * np + col] = x;
+    }
+  }
+  for (; jj < ny; ++jj) {
+    const double2 v = R[(size_t)jj * np + col];
+    x = double2{(v.x - a1[jj] * x.x) * a2[jj], (v.y - a1[jj] * x.y) * a2[jj]};
+    R[(size_t)jj * np + col] = x;
+  }
+  U[(size_t)(ny - 1) * np + col] = x;
+  jj = ny - 2;
+  for (; jj - 3 >= 0; jj -= 4) {
+    double2 v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = R[(size_t)(jj - q) * np + col];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const double b3 = a3[jj - q];
+      x = double2{v[q].x - b3 * x.x, v[q].y - b3 * x.y};
+      U[(size_t)(jj - q) * np + col] = x;
+    }
+  }
+  for (; jj >= 0; --jj) {
+    const double2 v = R[(size_t)jj * np + col];
+    x = double2{v.x - a3[jj] * x.x, v.y - a3[jj] * x.y};
+    U[(size_t)jj * np + col] = x;
+  }
+}
+
+void launch_vsolve(double2* r1, double2* r2, double2* r3, double2* u1, double2* u2, double2* u3, const Dims& d,
+                   const Tables& t, int k, cudaStream_t st) {
+  dim3 grid((d.np + 127) / 128, 3);
+  k_vsolve<<<grid, 128, 0, st>>>(r1, r2, r3, u1, u2, u3, d, t, k);
+}
+
+// flowrate_corr on mode (0,0): the flow-rate sum runs in the reference's
+// order on one thread; the correction is spread over the block.
+__global__ void k_flowrate(double2* u1, DevScalars* sc, Dims d, Tables t, int k, double Qx1) {
+  __shared__ double gsh;
+  if (threadIdx.x == 0) {
+    double Q = 0.0;
+    for (int j = 1; j <= d.nn + 1; ++j) Q = Q + t.dyvw[j] * u1[(size_t)(j - d.ju0) * d.np].x;
+    const double g = (sc->QxT - Q) / Qx1;
+    sc->Qx = Q;
+    sc->mpgx = sc->mpgx + g;
+    gsh = g;
+  }
+  __syncthreads();
+  const double g = gsh;
+  const double* u11 = t.u11 + (size_t)k * (d.nn + 3);
+  for (int j = threadIdx.x; j <= d.nn + 2; j += blockDim.x) {
+    double2* u = u1 + (size_t)(j - d.ju0) * d.np;
+    u->x = u->x + g * u11[j];
+  }
+}
+
+void launch_flowrate(double2* u1, DevScalars* sc, const Dims& d, const Tables& t, int k, double Qx1, cudaStream_t st) {
+  k_flowrate<<<1, 256, 0, st>>>(u1, sc, d, t, k, Qx1);
+}
+
+// LU_buildP + LU_decP (tridLU_3D_IB.f90:497-571,643-684), one thread per
+// column.  rows holds, per p level, the six products the matrix is made of:
+// [0] D_b(j-1)*G_t(j)  [1] D_t(j)*G_b(j)  [2] D_b(j-1)*G_b(j-1)  [3] D_t(j)*G_t(j+1).
+__global__ void k_build_dg(double* dg2, double* dg3, const double* rows, Dims d, Tables t, double pin) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= d.np) return;
+  const int i = col % d.nkx, kk = col / d.nkx;
+  const double k2x = t.k2x[i], k2z = t.k2z[kk];
+  const int ne = d.nyp - 1;
+  const size_t np = d.np;
+  // first row
+  double a2 = rows[1] + k2x + k2z;
+  double a3 = rows[3];
+  if (col == 0) { a2 = pin; a3 = 0.0; }
+  a2 = 1.0 / a2;
+  dg2[col] = a2;
+  for (int jp = 1; jp <= ne; ++jp) {
+    a3 = a3 * a2;                       // scaled upper diagonal of row jp-1
+    dg3[(size_t)(jp - 1) * np + col] = a3;
+    const double* q = rows + 4 * (size_t)jp;
+    const double b2 = (jp < ne) ? (q[0] + q[1]) + k2x + k2z : q[0] + k2x + k2z;
+    a2 = 1.0 / (b2 - q[2] * a3);
+    dg2[(size_t)jp * np + col] = a2;
+    a3 = (jp < ne) ? q[3] : 0.0;
+  }
+  dg3[(size_t)ne * np + col] = 0.0;
+}
+
+void launch_build_dg(double* dg2, double* dg3, const double* rows, const Dims& d, const Tables& t, double pin,
+                     cudaStream_t st) {
+  k_build_dg<<<(d.np + 127) / 128, 128, 0, st>>>(dg2, dg3, rows, d, t, pin);
+}
+
+// solveP + v_corr per column.
+__global__ void __launch_bounds__(128) k_psolve(double2* u1, double2* u2, double2* u3, double2* p, double2* psi,
+                                                Dims d, Tables t, double dtirk, double dtrk, double gwb,
+                                                double gwt) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= d.np) return;
+  const size_t np = d.np;
+  const int i = col % d.nkx, kk = col / d.nkx;
+  const double kx = t.kx[i], kz = t.kz[kk];
+  const int nyp = d.nyp;
+  double2 x = double2{0.0, 0.0};
+  for (int jp = 0; jp < nyp; ++jp) {
+    const int ju = jp + 1;
+    const double2 a = u1[(size_t)ju * np + col], w = u3[(size_t)ju * np + col];
+    const double2 v1 = u2[(size_t)ju * np + col], v0 = u2[(size_t)jp * np + col];
+    const double c = t.cu[ju];
+    double2 dv = double2{(-kx * a.y - kz * w.y) + c * (v1.x - v0.x), (kx * a.x + kz * w.x) + c * (v1.y - v0.y)};
+    double2 ps = double2{dtirk * dv.x, dtirk * dv.y};
+    if (col == 0 && jp == 0) ps = double2{0.0, 0.0};
+    const double b2 = t.dg2[(size_t)jp * np + col];
+    if (jp == 0) x = double2{ps.x * b2, ps.y * b2};
+    else {
+      const double b1 = t.dg1[jp];
+      x = double2{(ps.x - b1 * x.x) * b2, (ps.y - b1 * x.y) * b2};
+    }
+    psi[(size_t)jp * np + col] = x;
+  }
+  const double kxd = dtrk * kx, kzd = dtrk * kz;
+  double2 xn = x;  // psi(nyp-1)
+  for (int jp = nyp - 1; jp >= 0; --jp) {
+    double2 xc;
+    if (jp == nyp - 1) xc = xn;
+    else {
+      const double2 v = psi[(size_t)jp * np + col];
+      const double b3 = t.dg3[(size_t)jp * np + col];
+      xc = double2{v.x - b3 * xn.x, v.y - b3 * xn.y};
+    }
+    const size_t cp = (size_t)jp * np + col, cu = (size_t)(jp + 1) * np + col;
+    double2 pp = p[cp];
+    p[cp] = double2{pp.x + xc.x, pp.y + xc.y};
+    double2 a = u1[cu];
+    u1[cu] = double2{a.x - (-kxd * xc.y), a.y - (kxd * xc.x)};
+    double2 w = u3[cu];
+    u3[cu] = double2{w.x - (-kzd * xc.y), w.y - (kzd * xc.x)};
+    if (jp <= nyp - 2) {
+      const double f = dtrk * t.cv[jp + 1];
+      double2 v = u2[cu];
+      u2[cu] = double2{v.x - f * (xn.x - xc.x), v.y - f * (xn.y - xc.y)};
+    }
+    xn = xc;
+  }
+  u2[col] = double2{0.0, 0.0};
+  u2[(size_t)(d.nyv - 1) * np + col] = double2{0.0, 0.0};
+  {
+    const double2 a = u1[np + col], w = u3[np + col];
+    u1[col] = double2{-gwb * a.x, -gwb * a.y};
+    u3[col] = double2{-gwb * w.x, -gwb * w.y};
+    const double2 at = u1[(size_t)(d.nyu - 2) * np + col], wt = u3[(size_t)(d.nyu - 2) * np + col];
+    u1[(size_t)(d.nyu - 1) * np + col] = double2{-gwt * at.x, -gwt * at.y};
+    u3[(size_t)(d.nyu - 1) * np + col] = double2{-gwt * wt.x, -gwt * wt.y};
+  }
+}
+
+void launch_psolve(double2* u1, double2* u2, double2* u3, double2* p, double2* psi, const Dims& d, const Tables& t,
+                   double dtirk, double dtrk, double gwb, double gwt, cudaStream_t st) {
+  dim3 grid((d.np + 127) / 128);
+  k_psolve<<<grid, 128, 0, st>>>(u1, u2, u3, p, psi, d, t, dtirk, dtrk, gwb, gwt);
+}
+
+__global__ void k_divergence(const double2* u1, const double2* u2, const double2* u3, double2* div, Dims d, Tables t) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= d.np) return;
+  const int jp = blockIdx.y, ju = jp + 1;
+  const size_t np = d.np;
+  const int i = col % d.nkx, kk = col / d.nkx;
+  const double kx = t.kx[i], kz = t.kz[kk];
+  const double2 a = u1[(size_t)ju * np + col], w = u3[(size_t)ju * np + col];
+  const double2 v1 = u2[(size_t)ju * np + col], v0 = u2[(size_t)jp * np + col];
+  const double c = t.cu[ju];
+  div[(size_t)jp * np + col] =
+      double2{(-kx * a.y - kz * w.y) + c * (v1.x - v0.x), (kx * a.x + kz * w.x) + c * (v1.y - v0.y)};
+}
+
+void launch_divergence(const double2* u1, const double2* u2, const double2* u3, double2* div, const Dims& d,
+                       const Tables& t, cudaStream_t st) {
+  dim3 grid((d.np + 255) / 256, d.nyp);
+  k_divergence<<<grid, 256, 0, st>>>(u1, u2, u3, div, d, t);
+}
+
+__global__ void k_absmax(const double2* x, size_t n, DevScalars* sc) {
+  double m = 0.0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    m = fmax(m, hypot(x[e].x, x[e].y));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(&sc->cflbits, (unsigned long long)__double_as_longlong(m));
+}
+
+void launch_absmax(const double2* x, size_t n, DevScalars* sc, cudaStream_t st) {
+  k_absmax<<<152 * 4, 256, 0, st>>>(x, n, sc);
+}
+
+// [rows][cols] -> [cols][rows] through a shared-memory tile.
+__global__ void k_transpose(const double2* __restrict__ src, double2* __restrict__ dst, int rows, int cols) {
+  __shared__ double2 tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int row = by + r, c = bx + threadIdx.x;
+    if (row < rows && c < cols) tile[r][threadIdx.x] = src[(size_t)row * cols + c];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int c = bx + r, row = by + threadIdx.x;
+    if (row < rows && c < cols) dst[(size_t)c * rows + row] = tile[threadIdx.x][r];
+  }
+}
+
+void launch_transpose(const double2* src, double2* dst, int rows, int cols, cudaStream_t st) {
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32);
+  k_transpose<<<grid, dim3(32, 8), 0, st>>>(src, dst, rows, cols);
+}
+
+// spectra.f90:18-56: sums of |u|^2, |v|^2, |w|^2, Re(u conj v_c), |p|^2 per (level, column).
+// sp layout: [spU nyu][spV nyv][spW nyu][spUV nyu][spP nyp] planes of np doubles.
+__global__ void k_spectra(const double2* u1, const double2* u2, const double2* u3, const double2* p, double* sp,
+                          Dims d, Tables t) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= d.np) return;
+  const int jj = blockIdx.y;
+  const size_t np = d.np;
+  double* spU = sp;
+  double* spV = spU + (size_t)d.nyu * np;
+  double* spW = spV + (size_t)d.nyv * np;
+  double* spUV = spW + (size_t)d.nyu * np;
+  double* spP = spUV + (size_t)d.nyu * np;
+  const size_t c0 = (size_t)jj * np + col;
+  if (jj < d.nyu) {
+    const double2 a = u1[c0], w = u3[c0];
+    spU[c0] = spU[c0] + a.x * a.x + a.y * a.y;
+    spW[c0] = spW[c0] + w.x * w.x + w.y * w.y;
+    double2 vi = double2{0.0, 0.0};
+    if (jj >= 1 && jj <= d.nyu - 2) {
+      const double2 v0 = u2[c0 - np], v1 = u2[c0];
+      const double wc = t.wc[jj];
+      vi = double2{v0.x + wc * (v1.x - v0.x), v0.y + wc * (v1.y - v0.y)};
+    }
+    spUV[c0] = spUV[c0] + a.x * vi.x + a.y * vi.y;
+  }
+  if (jj < d.nyv) {
+    const double2 v = u2[c0];
+    spV[c0] = spV[c0] + v.x * v.x + v.y * v.y;
+  }
+  if (jj < d.nyp) {
+    const double2 q = p[c0];
+    spP[c0] = spP[c0] + q.x * q.x + q.y * q.y;
+  }
+}
+
+void launch_spectra(const double2* u1, const double2* u2, const double2* u3, const double2* p, double* sp,
+                    const Dims& d, const Tables& t, cudaStream_t st) {
+  dim3 grid((d.np + 255) / 256, d.nyu);
+  k_spectra<<<grid, 256, 0, st>>>(u1, u2, u3, p, sp, d, t);
+}
+
+// Large dynamic shared memory for the transform kernels (one call per process).
+void configure_kernels() {
+  static bool done = false;
+  if (done) return;
+  done = true;
+  const int mx = 227 * 1024;
+  cudaFuncSetAttribute(k_zinv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_zinv<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_zfwd<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_zfwd<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_xprod<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_xprod<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_xmask<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_xmask<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+}
+
+template void launch_zinv<double>(const ZJobs<double>&, const Dims&, const FftPlan&, int, cudaStream_t);
+template void launch_zinv<float>(const ZJobs<float>&, const Dims&, const FftPlan&, int, cudaStream_t);
+template void launch_zfwd<double>(const ZJobs<double>&, const Dims&, const FftPlan&, int, double, cudaStream_t);
+template void launch_zfwd<float>(const ZJobs<float>&, const Dims&, const FftPlan&, int, double, cudaStream_t);
+template void launch_xprod<double>(const ProdArgs<double>&, const Dims&, const FftPlan&, const double2*, cudaStream_t);
+template void launch_xprod<float>(const ProdArgs<float>&, const Dims&, const FftPlan&, const double2*, cudaStream_t);
+template void launch_xmask<double>(const MaskArgs<double>&, const Dims&, const FftPlan&, const double2*, cudaStream_t);
+template void launch_xmask<float>(const MaskArgs<float>&, const Dims&, const FftPlan&, const double2*, cudaStream_t);
+
+}  // namespace lh
+

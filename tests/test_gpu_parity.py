@@ -1,0 +1,124 @@
+"""GPU parity: the CUDA RK3 step against the CPU FP64 oracle on the same inputs.
+
+Every test builds both from one configuration, feeds them the same projected
+seeded field and compares with relative L2 norms.  The FP64 bar is 1e-10 after
+10 RK3 steps (the tolerance of the target), tighter for single substages.
+"""
+import numpy as np
+import pytest
+
+from tests.helpers import C1, SMALL, SMOOTH, projected_ic, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+SUBSTAGE_TOL = 1e-11
+STEP10_TOL = 1e-10
+
+
+def _pair(po, cfg, precision=0, seed=1):
+    import littleharsh_gb300 as lh
+    o = po.Oracle(**cfg)
+    u1, u2, u3, p = projected_ic(o, seed=seed)
+    dt = o.cfl_dt(0.5)
+    Q = o.flowrate()
+    o.set_fields(u1, u2, u3, p)
+    o.set_scalars(0.0, dt, 0.0, Q)
+    s = lh.Solver(lh.Config(**cfg), precision=precision)
+    s.set_fields(u1, u2, u3, p)
+    s.set_time(0.0, dt, 0.0, Q)
+    return o, s
+
+
+def _cmp_fields(o, s, tol, what=""):
+    fo = o.get_fields()
+    fs = s.get_fields()
+    for name, a, b in zip(("u1", "u2", "u3", "p"), fs, fo):
+        e = rel_l2(a, b)
+        assert e < tol, f"{what} {name}: rel L2 {e:.3e} >= {tol:.1e}"
+
+
+@pytest.mark.parametrize("cfg", [SMALL, SMOOTH], ids=["canopy24", "smooth24"])
+@pytest.mark.parametrize("upto", [1, 2, 3, 4, 5])
+def test_substage_stages(oracle_mod, cfg, upto):
+    o, s = _pair(oracle_mod, cfg)
+    o.substage(1, upto)
+    s.substage(1, upto)
+    if upto <= 2:
+        for name, a, b in zip(("r1", "r2", "r3"), s.get_rhs(), o.get_rhs()):
+            assert rel_l2(a, b) < SUBSTAGE_TOL, f"stage {upto} {name}: {rel_l2(a, b):.3e}"
+        for name, a, b in zip(("n1", "n2", "n3"), s.get_nonlinear(), o.get_nonlinear()):
+            assert rel_l2(a, b) < SUBSTAGE_TOL, f"stage {upto} {name}: {rel_l2(a, b):.3e}"
+    else:
+        _cmp_fields(o, s, SUBSTAGE_TOL, f"stage {upto}")
+    if upto >= 4:
+        assert abs(s.time()["mpgx"] - o.scalars()["mpgx"]) < 1e-10 * max(1.0, abs(o.scalars()["mpgx"]))
+
+
+def test_three_substages_sequence(oracle_mod):
+    o, s = _pair(oracle_mod, SMALL)
+    for k in (1, 2, 3):
+        o.substage(k, 5)
+        s.substage(k, 5)
+        _cmp_fields(o, s, SUBSTAGE_TOL, f"after kRK={k}")
+
+
+@pytest.mark.parametrize("cfg", [SMALL, C1], ids=["canopy24", "config1_96x97"])
+def test_ten_steps_fp64(oracle_mod, cfg):
+    o, s = _pair(oracle_mod, cfg)
+    o.step(10)
+    s.step(10)
+    _cmp_fields(o, s, STEP10_TOL, "10 steps")
+    assert abs(s.time()["mpgx"] - o.scalars()["mpgx"]) < 1e-9 * abs(o.scalars()["mpgx"])
+    assert s.divmax() < 1e-9
+
+
+def test_mixed_precision_close(oracle_mod):
+    import littleharsh_gb300 as lh
+    o, s = _pair(oracle_mod, SMALL, precision=lh.PREC_MIXED)
+    o.step(10)
+    s.step(10)
+    fo, fs = o.get_fields(), s.get_fields()
+    for name, a, b in zip(("u1", "u2", "u3"), fs, fo):
+        e = rel_l2(a, b)
+        assert e < 1e-4, f"mixed {name}: {e:.3e}"
+    assert s.divmax() < 1e-9  # the projection stays FP64
+
+
+def test_column_layout_roundtrip(oracle_mod):
+    import littleharsh_gb300 as lh
+    o, s = _pair(oracle_mod, SMALL)
+    u1, u2, u3, p = s.get_fields(lh.LAYOUT_PLANES)
+    c = s.get_fields(lh.LAYOUT_COLUMNS)
+    # reference cfield f(j, column): column = kk*nkx + i, j fastest
+    np.testing.assert_array_equal(c[0], u1.reshape(u1.shape[0], -1).T)
+    np.testing.assert_array_equal(c[3], p.reshape(p.shape[0], -1).T)
+    s.set_fields(*c, layout=lh.LAYOUT_COLUMNS)
+    back = s.get_fields(lh.LAYOUT_PLANES)
+    for a, b in zip(back, (u1, u2, u3, p)):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_divergence_and_cfl(oracle_mod):
+    o, s = _pair(oracle_mod, SMALL)
+    assert abs(s.divmax() - o.divmax()) < 1e-12
+    assert abs(s.cfl_dt(0.5) - o.cfl_dt(0.5)) < 1e-12 * o.cfl_dt(0.5)
+
+
+def test_spectra(oracle_mod):
+    o, s = _pair(oracle_mod, SMALL)
+    o.step(2)
+    s.step(2)
+    o.spectra_accumulate()
+    s.spectra_accumulate()
+    n, sg = s.spectra_flush()
+    so = o.spectra()
+    assert n == 1
+    for a, b in zip(sg, so):
+        assert rel_l2(a, b) < 1e-10
+
+
+def test_step_is_graph_replay(oracle_mod):
+    o, s = _pair(oracle_mod, SMALL)
+    s.step(3)
+    ms, launches = s.last_step_ms()
+    assert ms > 0 and launches > 0
