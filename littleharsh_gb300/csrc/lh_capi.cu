@@ -658,7 +658,10 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
   h->tx = d.ngz * 16 * (int)sizeof(double2) <= 160 * 1024 ? 16 : 8;
   if (h->precision == LH_PREC_MIXED && d.ngz * 32 * (int)sizeof(float2) <= 160 * 1024) h->tx = 32;
   h->chunk = d.nyu > 256 ? 32 : 16;
-  configure_kernels();
+  {
+    const cudaError_t e = configure_kernels();
+    if (e != cudaSuccess) return bail(fail(h, LH_ECUDA, "kernel attributes: %s", cudaGetErrorString(e)));
+  }
   if (cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
     return bail(fail(h, LH_ECUDA, "cudaEventCreate failed"));
   {

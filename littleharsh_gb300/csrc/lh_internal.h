@@ -136,6 +136,6 @@ void launch_absmax(const double2* x, size_t n, DevScalars* sc, cudaStream_t st);
 void launch_transpose(const double2* src, double2* dst, int rows, int cols, cudaStream_t st);
 void launch_spectra(const double2* u1, const double2* u2, const double2* u3, const double2* p, double* sp,
                     const Dims& d, const Tables& t, cudaStream_t st);
-void configure_kernels();
+cudaError_t configure_kernels();
 
 }  // namespace lh

@@ -755,20 +755,33 @@ void launch_spectra(const double2* u1, const double2* u2, const double2* u3, con
   k_spectra<<<grid, 256, 0, st>>>(u1, u2, u3, p, sp, d, t);
 }
 
-// Large dynamic shared memory for the transform kernels (one call per process).
-void configure_kernels() {
-  static bool done = false;
-  if (done) return;
-  done = true;
-  const int mx = 227 * 1024;
-  cudaFuncSetAttribute(k_zinv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_zinv<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_zfwd<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_zfwd<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_xprod<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_xprod<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_xmask<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_xmask<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+// Opt the transform kernels in to the largest dynamic shared memory the
+// device allows next to their static shared memory (once per device).
+template <typename K>
+static cudaError_t allow_smem(K kernel, int optin) {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+}
+
+cudaError_t configure_kernels() {
+  static unsigned long long done = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 64 && (done >> dev & 1ull)) return cudaSuccess;
+  int optin = 0;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  const cudaError_t r[8] = {allow_smem(k_zinv<double>, optin), allow_smem(k_zinv<float>, optin),
+                            allow_smem(k_zfwd<double>, optin), allow_smem(k_zfwd<float>, optin),
+                            allow_smem(k_xprod<double>, optin), allow_smem(k_xprod<float>, optin),
+                            allow_smem(k_xmask<double>, optin), allow_smem(k_xmask<float>, optin)};
+  for (cudaError_t x : r)
+    if (x != cudaSuccess) return x;
+  if (dev < 64) done |= 1ull << dev;
+  return cudaSuccess;
 }
 
 template void launch_zinv<double>(const ZJobs<double>&, const Dims&, const FftPlan&, int, cudaStream_t);
