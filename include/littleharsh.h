@@ -165,6 +165,25 @@ int lh_last_step_ms(lh_handle* h, double* ms, int32_t* launches_per_step);
  * nkinds must be at least 10. */
 int lh_profile_step(lh_handle* h, double* ms_by_kind, int32_t* count_by_kind, int32_t nkinds);
 
+/* Divergence-free projection (solveP + v_corr with kRK = 1, the operation of
+ * lh_project) of caller-owned device arrays u1, u2, u3 (plane layout), for
+ * callers that cannot allocate device memory: a Fortran driver whose fields
+ * live in OpenACC or CUDA Fortran device arrays, or an application that owns
+ * all GPU memory through one arena and must not call cudaMalloc mid-run.
+ * No counterpart in the reference.  It needs no handle and allocates nothing:
+ * its scratch (wavenumbers, metric, pressure LU, psi, p) is a 64 MiB static
+ * device array that every GPU loading the library holds until exit, which
+ * limits the grid to about 48 bytes x nyp x (N1/2+1) x N2 <= 64 MiB
+ * (configuration 1 fits, configuration 2 does not); larger grids return
+ * LH_EINVAL with the reason in lh_last_error(NULL).  prm, yu, dthdyu and
+ * dthdyv are the host arrays lh_init takes; dt only scales psi (it cancels).
+ * The first call on a device looks up the array's device address, so make it
+ * before any stream capture.  All calls share the array: calls whose work
+ * overlaps on the GPU race.  Runs on `stream` (cudaStream_t, NULL = default)
+ * of the current device and returns after the projection has finished. */
+int lh_project_noalloc(const lh_params* prm, const double* yu, const double* dthdyu, const double* dthdyv,
+                       double* u1, double* u2, double* u3, double dt, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Host helpers restating the setup the Fortran driver does in start.f90, for
  * drivers without a Fortran compiler.

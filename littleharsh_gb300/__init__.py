@@ -30,7 +30,7 @@ EXPORTED_SYMBOLS = [
     "lh_init", "lh_free", "lh_last_error", "lh_get_sizes", "lh_set_fields", "lh_get_fields", "lh_set_nonlinear",
     "lh_get_nonlinear", "lh_set_time", "lh_get_time", "lh_rk3_step", "lh_substage", "lh_get_rhs", "lh_divmax",
     "lh_cfl_dt", "lh_project", "lh_spectra_accumulate", "lh_spectra_flush", "lh_stats_accumulate",
-    "lh_stats_flush", "lh_last_step_ms", "lh_profile_step", "lh_read_input", "lh_setup_grid", "lh_setup_canopy",
+    "lh_stats_flush", "lh_last_step_ms", "lh_profile_step", "lh_project_noalloc", "lh_read_input", "lh_setup_grid", "lh_setup_canopy",
 ]
 
 
@@ -110,6 +110,7 @@ def load_library(build: bool = True) -> C.CDLL:
     L.lh_stats_flush.argtypes = [vp, _dp, C.POINTER(i32), i32]
     L.lh_last_step_ms.argtypes = [vp, _dp, C.POINTER(i32)]
     L.lh_profile_step.argtypes = [vp, _dp, C.c_void_p, i32]
+    L.lh_project_noalloc.argtypes = [C.POINTER(Params)] + [_dp] * 3 + [C.c_void_p] * 3 + [C.c_double, C.c_void_p]
     L.lh_read_input.argtypes = [cp, C.POINTER(Input)]
     L.lh_setup_grid.argtypes = [C.POINTER(Input), C.POINTER(Params)] + [_dp] * 6
     L.lh_setup_canopy.argtypes = [C.POINTER(Input), C.POINTER(Params), C.c_void_p, C.POINTER(i32), C.c_void_p,

@@ -437,6 +437,10 @@ int host_flowrate(lh_handle* h, double* Q) {
 
 }  // namespace
 
+namespace lh {
+void set_init_error(const char* msg) { g_init_error = msg; }
+}  // namespace lh
+
 extern "C" {
 
 const char* lh_last_error(const lh_handle* h) { return h ? h->err.c_str() : g_init_error.c_str(); }

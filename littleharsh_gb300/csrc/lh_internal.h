@@ -138,4 +138,7 @@ void launch_spectra(const double2* u1, const double2* u2, const double2* u3, con
                     const Dims& d, const Tables& t, cudaStream_t st);
 cudaError_t configure_kernels();
 
+// Message returned by lh_last_error(NULL) on this thread (lh_capi.cu).
+void set_init_error(const char* msg);
+
 }  // namespace lh
