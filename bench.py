@@ -38,6 +38,10 @@ WORKLOADS = {
     "config1_96x96x130_fp64": dict(Re=2800.0, alp=1.0, bet=2.0, ngalx=96, ngalz=96, ny=97, dyq=13.6, ppp=5,
                                    geometry_type=3, posth=0.2, dsty=16, dstx=2, dstz=4, ntilex=12, ntilez=6,
                                    flag_ctpress=0),
+    # mid-size case for ncu captures: inputs of the x pass larger than L2, ~2 GB on the device
+    "mid_288x288x226_fp64": dict(Re=5000.0, alp=1.0, bet=2.0, ngalx=288, ngalz=288, ny=193, dyq=13.6, ppp=5,
+                                 geometry_type=3, posth=0.1, dsty=16, dstx=4, dstz=4, ntilex=24, ntilez=12,
+                                 flag_ctpress=0),
 }
 DEFAULT_WORKLOAD = "config2_576x576x450_fp64"
 METRIC = "grid-pt RK3 steps/s"

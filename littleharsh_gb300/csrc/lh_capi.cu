@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -659,9 +660,13 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
     if ((rc = dalloc(h, &h->spec, (3 * (size_t)d.nyu + d.nyv + d.nyp) * d.np))) return bail(rc);
   }
   // launch shapes: z tile width and levels per x-pass chunk
-  h->tx = d.ngz * 16 * (int)sizeof(double2) <= 160 * 1024 ? 16 : 8;
-  if (h->precision == LH_PREC_MIXED && d.ngz * 32 * (int)sizeof(float2) <= 160 * 1024) h->tx = 32;
+  // z tile width: narrow tiles keep several CTAs per SM so that one CTA's loads overlap another's
+  // butterflies (measured on configuration 2: FP64 best at 4, mixed at 8)
+  h->tx = h->precision == LH_PREC_MIXED ? 8 : 4;
   h->chunk = d.nyu > 256 ? 32 : 16;
+  // launch-shape overrides for tuning sweeps: LH_TX (z tile width, 1..64), LH_CHUNK (levels per x-pass CTA)
+  if (const char* v = std::getenv("LH_TX")) { const int x = std::atoi(v); if (x >= 1 && x <= 64) h->tx = x; }
+  if (const char* v = std::getenv("LH_CHUNK")) { const int x = std::atoi(v); if (x >= 1 && x <= 4096) h->chunk = x; }
   {
     const cudaError_t e = configure_kernels();
     if (e != cudaSuccess) return bail(fail(h, LH_ECUDA, "kernel attributes: %s", cudaGetErrorString(e)));
