@@ -79,6 +79,7 @@ typedef struct lh_params {
   double ddthetavi;        /* 1/dtheta from y_grid_canopy (1 in the reference) */
   double gridweighting[6]; /* gridweighting(1:3,1:2), Fortran order (start.f90:497-503) */
   int32_t precision;       /* LH_PREC_FP64 or LH_PREC_MIXED */
+  int32_t ntilex, ntilez;  /* canopy tiles in x and z (input.in), for the conditional statistics */
   int32_t reserved;
   void* stream;            /* cudaStream_t, NULL = default stream */
 } lh_params;
@@ -147,11 +148,29 @@ int lh_spectra_accumulate(lh_handle* h);
 int lh_spectra_flush(lh_handle* h, double* spU, double* spV, double* spW, double* spUV, double* spP,
                      int32_t* count, int32_t reset);
 
-/* Plane statistics (stats.f90:1-108), FP64 sums over physical planes:
- * out is 13 x max(nyu, nyv): Um U2m Vm V2m Wm W2m Pm P2m UVm UWm VWm (rows
- * 11-12 reserved).  Rows on the v or p grid use their first nyv / nyp entries. */
+/* Plane statistics (stats.f90:1-108), FP64 sums over the physical planes of
+ * each level: out is 13 x max(nyu, nyv): Um U2m Vm V2m Wm W2m Pm P2m UVm UWm
+ * VWm (rows 11-12, omega_x, are reserved and stay zero).  Rows on the v or p
+ * grid use their first nyv / nyp entries.  UVm pairs u with v interpolated to
+ * the centres, VWm v with w interpolated to the faces (both zero on ghost
+ * centres / wall faces).  The sums are formed from the spectral coefficients
+ * (Parseval on the 3/2 grid), equal to the physical sums up to rounding.
+ * Call between steps: it reuses the right-hand-side scratch. */
 int lh_stats_accumulate(lh_handle* h);
 int lh_stats_flush(lh_handle* h, double* out, int32_t* count, int32_t reset);
+
+/* Conditional statistics of the wall bands (conddown1/2 and condup1/2,
+ * stats.f90:110-253): sums over the ntilex x ntilez canopy tiles at each
+ * in-tile point (dnx = Ngalx/ntilex by dnz = Ngalz/ntilez), for the planes of
+ * the bottom band counted from its wall plus those of the top band counted
+ * from the top wall with v's sign flipped (write_stats sums the two,
+ * stats.f90:473-512), accumulated in FP64 from physical planes.  dims[0..4] =
+ * nju, njv, njp, dnx, dnz (nju = N(4,1)-N(4,0)+1, njv = N(3,1)-N(3,0)+1,
+ * njp = N(4,1)-N(4,0)-1; all 0 without canopies).  out: 11 blocks
+ * [j1][kin][i] (i fastest): UmC U2mC WmC W2mC UVmC UWmC (nju planes), VmC
+ * V2mC VWmC (njv), PmC P2mC (njp).  Call between steps. */
+int lh_cond_accumulate(lh_handle* h);
+int lh_cond_flush(lh_handle* h, double* out, int32_t* dims5, int32_t* count, int32_t reset);
 
 /* Device time of the last lh_rk3_step call in milliseconds (CUDA events on
  * the handle's stream) and the number of kernels one step launches. */
@@ -183,6 +202,32 @@ int lh_profile_step(lh_handle* h, double* ms_by_kind, int32_t* count_by_kind, in
  * of the current device and returns after the projection has finished. */
 int lh_project_noalloc(const lh_params* prm, const double* yu, const double* dthdyu, const double* dthdyv,
                        double* u1, double* u2, double* u3, double dt, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * The reference's files.  Fortran sequential unformatted records (4-byte
+ * length before and after each record).
+ * ------------------------------------------------------------------------- */
+
+/* Restart fields in the format read_in reads (start.f90:1786-2235): files
+ * <dir>/u1<name>, u2<name>, u3<name>, p<name> (name = fnameimb(3:) in the
+ * reference); records: header (t, Re, alp, bet, mpgx, nband, iter, 88 ints),
+ * N(4,0:4), one record read_in skips (the field's y coordinates), then one
+ * record per plane of the field's grid: jin, band, nx = N1+2, nz = N2, y(jin),
+ * buffSR(nx, nz) -- the packed x half-spectrum of the plane's z modes.
+ * prm is the block given to lh_init; yu, yv its grid arrays. */
+int lh_write_restart(lh_handle* h, const lh_params* prm, const double* yu, const double* yv, const char* dir,
+                     const char* name, int32_t iter);
+/* Read the four files (the grid must match: LH_EUNSUPPORTED otherwise) and
+ * upload them as lh_set_fields does (QxT from u1 for constant flow rate). */
+int lh_read_restart(lh_handle* h, const char* dir, const char* name, double* t_out, int32_t* iter_out);
+/* write_stats (stats.f90:355-410) of the accumulated plane and conditional
+ * statistics to `path`; resets the accumulators as write_stats does. */
+int lh_write_stats(lh_handle* h, const lh_params* prm, const double* yu, const double* yv, const double* dthdyu,
+                   const double* dthdyv, const char* path, int32_t iter);
+/* recvwrspec (spectra.f90:109-180): <dir>/spU_<name> ... spP_<name>, kz and
+ * -kz folded and kx >= 1 doubled; resets the accumulators. */
+int lh_write_spectra(lh_handle* h, const lh_params* prm, const double* yu, const double* yv, const double* dthdyu,
+                     const double* dthdyv, const char* dir, const char* name, int32_t iter);
 
 /* ---------------------------------------------------------------------------
  * Host helpers restating the setup the Fortran driver does in start.f90, for

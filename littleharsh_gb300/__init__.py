@@ -30,7 +30,8 @@ EXPORTED_SYMBOLS = [
     "lh_init", "lh_free", "lh_last_error", "lh_get_sizes", "lh_set_fields", "lh_get_fields", "lh_set_nonlinear",
     "lh_get_nonlinear", "lh_set_time", "lh_get_time", "lh_rk3_step", "lh_substage", "lh_get_rhs", "lh_divmax",
     "lh_cfl_dt", "lh_project", "lh_spectra_accumulate", "lh_spectra_flush", "lh_stats_accumulate",
-    "lh_stats_flush", "lh_last_step_ms", "lh_profile_step", "lh_project_noalloc", "lh_read_input", "lh_setup_grid", "lh_setup_canopy",
+    "lh_stats_flush", "lh_cond_accumulate", "lh_cond_flush", "lh_last_step_ms", "lh_profile_step",
+    "lh_project_noalloc", "lh_write_restart", "lh_read_restart", "lh_write_stats", "lh_write_spectra", "lh_read_input", "lh_setup_grid", "lh_setup_canopy",
 ]
 
 
@@ -43,8 +44,8 @@ class Params(C.Structure):
         ("abi_version", C.c_int32), ("N", C.c_int32 * 20), ("Ngal", C.c_int32 * 20), ("nn", C.c_int32),
         ("flag_ctpress", C.c_int32), ("geometry_type", C.c_int32), ("dsty", C.c_int32),
         ("Re", C.c_double), ("alp", C.c_double), ("bet", C.c_double), ("ddthetavi", C.c_double),
-        ("gridweighting", C.c_double * 6), ("precision", C.c_int32), ("reserved", C.c_int32),
-        ("stream", C.c_void_p),
+        ("gridweighting", C.c_double * 6), ("precision", C.c_int32), ("ntilex", C.c_int32),
+        ("ntilez", C.c_int32), ("reserved", C.c_int32), ("stream", C.c_void_p),
     ]
 
 
@@ -108,9 +109,15 @@ def load_library(build: bool = True) -> C.CDLL:
     L.lh_spectra_flush.argtypes = [vp] + [_dp] * 5 + [C.POINTER(i32), i32]
     L.lh_stats_accumulate.argtypes = [vp]
     L.lh_stats_flush.argtypes = [vp, _dp, C.POINTER(i32), i32]
+    L.lh_cond_accumulate.argtypes = [vp]
+    L.lh_cond_flush.argtypes = [vp, _dp, C.c_void_p, C.POINTER(i32), i32]
     L.lh_last_step_ms.argtypes = [vp, _dp, C.POINTER(i32)]
     L.lh_profile_step.argtypes = [vp, _dp, C.c_void_p, i32]
     L.lh_project_noalloc.argtypes = [C.POINTER(Params)] + [_dp] * 3 + [C.c_void_p] * 3 + [C.c_double, C.c_void_p]
+    L.lh_write_restart.argtypes = [vp, C.POINTER(Params), _dp, _dp, cp, cp, i32]
+    L.lh_read_restart.argtypes = [vp, cp, cp, _dp, C.POINTER(i32)]
+    L.lh_write_stats.argtypes = [vp, C.POINTER(Params)] + [_dp] * 4 + [cp, i32]
+    L.lh_write_spectra.argtypes = [vp, C.POINTER(Params)] + [_dp] * 4 + [cp, cp, i32]
     L.lh_read_input.argtypes = [cp, C.POINTER(Input)]
     L.lh_setup_grid.argtypes = [C.POINTER(Input), C.POINTER(Params)] + [_dp] * 6
     L.lh_setup_canopy.argtypes = [C.POINTER(Input), C.POINTER(Params), C.c_void_p, C.POINTER(i32), C.c_void_p,
@@ -315,6 +322,65 @@ class Solver:
 
     def project(self):
         self._check(load_library().lh_project(self.h))
+
+    STAT_ROWS = ("Um", "U2m", "Vm", "V2m", "Wm", "W2m", "Pm", "P2m", "UVm", "UWm", "VWm")
+
+    def stats_accumulate(self):
+        self._check(load_library().lh_stats_accumulate(self.h))
+
+    def stats_flush(self, reset: bool = True):
+        """(count, dict row -> profile over the row's own grid levels)."""
+        L = max(self.nyu, self.nyv)
+        o = np.zeros((13, L))
+        n = C.c_int32(0)
+        self._check(load_library().lh_stats_flush(self.h, _p(o), C.byref(n), int(reset)))
+        ny = dict(Um=self.nyu, U2m=self.nyu, Vm=self.nyv, V2m=self.nyv, Wm=self.nyu, W2m=self.nyu, Pm=self.nyp,
+                  P2m=self.nyp, UVm=self.nyu, UWm=self.nyu, VWm=self.nyv)
+        return n.value, {k: o[r, :ny[k]].copy() for r, k in enumerate(self.STAT_ROWS)}
+
+    COND_ROWS = ("UmC", "U2mC", "WmC", "W2mC", "UVmC", "UWmC", "VmC", "V2mC", "VWmC", "PmC", "P2mC")
+
+    def cond_accumulate(self):
+        self._check(load_library().lh_cond_accumulate(self.h))
+
+    def cond_flush(self, reset: bool = True):
+        """(count, dict name -> array [j1][kin][i]) of the conditional statistics."""
+        L = load_library()
+        dims = np.zeros(5, np.int32)
+        n = C.c_int32(0)
+        self._check(L.lh_cond_flush(self.h, None, dims.ctypes.data, C.byref(n), 0))
+        nju, njv, njp, dnx, dnz = [int(x) for x in dims]
+        sizes = [nju] * 6 + [njv] * 3 + [njp] * 2
+        out = np.zeros(max(sum(sizes) * dnx * dnz, 1))
+        self._check(L.lh_cond_flush(self.h, _p(out), dims.ctypes.data, C.byref(n), int(reset)))
+        res, off = {}, 0
+        for name, nj in zip(self.COND_ROWS, sizes):
+            res[name] = out[off:off + nj * dnx * dnz].reshape(nj, dnz, dnx)
+            off += nj * dnx * dnz
+        return n.value, res
+
+    # the reference's files -------------------------------------------------
+    def write_restart(self, directory: str, name: str, iteration: int = 0):
+        g = self.grid
+        self._check(load_library().lh_write_restart(self.h, C.byref(self.params), _p(g["yu"]), _p(g["yv"]),
+                                                    directory.encode(), name.encode(), iteration))
+
+    def read_restart(self, directory: str, name: str):
+        t, it = C.c_double(0), C.c_int32(0)
+        self._check(load_library().lh_read_restart(self.h, directory.encode(), name.encode(), C.byref(t),
+                                                   C.byref(it)))
+        return t.value, it.value
+
+    def write_stats(self, path: str, iteration: int = 0):
+        g = self.grid
+        self._check(load_library().lh_write_stats(self.h, C.byref(self.params), _p(g["yu"]), _p(g["yv"]),
+                                                  _p(g["dthdyu"]), _p(g["dthdyv"]), path.encode(), iteration))
+
+    def write_spectra(self, directory: str, name: str, iteration: int = 0):
+        g = self.grid
+        self._check(load_library().lh_write_spectra(self.h, C.byref(self.params), _p(g["yu"]), _p(g["yv"]),
+                                                    _p(g["dthdyu"]), _p(g["dthdyv"]), directory.encode(),
+                                                    name.encode(), iteration))
 
     def spectra_accumulate(self):
         self._check(load_library().lh_spectra_accumulate(self.h))

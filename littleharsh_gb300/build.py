@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "liblh_gb300.so")
-SOURCES = ["lh_kernels.cu", "lh_capi.cu", "lh_host.cpp", "lh_noalloc.cu"]
+SOURCES = ["lh_kernels.cu", "lh_capi.cu", "lh_host.cpp", "lh_noalloc.cu", "lh_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -66,6 +66,12 @@ struct lh_handle {
   uint8_t *ibu_mask = nullptr, *ibv_mask = nullptr;
   double* spec = nullptr;  // spectra accumulators
   int nspec = 0;
+  double* stat = nullptr;  // plane statistics accumulators, 13 rows of max(nyu, nyv)
+  int nstat = 0;
+  // conditional statistics: planes per grid, tile size, accumulators, level lists (both walls interleaved)
+  int nju = 0, njv = 0, njp = 0, dnx = 0, dnz = 0, ncond = 0;
+  double* cond = nullptr;
+  int *cond_ul = nullptr, *cond_vl = nullptr, *cond_pl = nullptr;
   double* tabs = nullptr;  // lu_u, lu_v, u11 (rewritten when dt changes)
   DevScalars* sc = nullptr;
   PlanStore pz, ph;
@@ -136,9 +142,10 @@ int upload(lh_handle* h, T** out, const std::vector<T>& v) {
   return LH_OK;
 }
 
-// Stages of a DIF sequence for length n: radix 3 first, then 2, radix 4 last
-// (the last stage needs no twiddles, which saves the most work on radix 4).
-int build_plan(lh_handle* h, PlanStore& ps, int n) {
+// Stages of a DIT sequence for length n: radix 4 first (stage 0 has no
+// twiddles, which saves the most on radix 4), then 2, radix 3 last (so that
+// the last stage splits the output in thirds, which the z-forward can prune).
+int build_plan(lh_handle* h, PlanStore& ps, int n, int keep_half) {
   FftPlan& P = ps.plan;
   std::memset(&P, 0, sizeof P);
   P.n = n;
@@ -148,20 +155,23 @@ int build_plan(lh_handle* h, PlanStore& ps, int n) {
   while (m % 3 == 0) { m /= 3; ++n3; }
   if (m != 1) return fail(h, LH_EFFT, "transform length %d does not factor into 2, 3 and 4", n);
   int s = 0;
-  for (int i = 0; i < n3; ++i) P.rad[s++] = 3;
-  for (int i = 0; i < n2; ++i) P.rad[s++] = 2;
   for (int i = 0; i < n4; ++i) P.rad[s++] = 4;
+  for (int i = 0; i < n2; ++i) P.rad[s++] = 2;
+  for (int i = 0; i < n3; ++i) P.rad[s++] = 3;
   if (s > kMaxStages) return fail(h, LH_EFFT, "transform length %d needs too many stages", n);
   P.ns = s;
-  int L = n;
-  for (int i = 0; i < s; ++i) { P.len[i] = L; L /= P.rad[i]; }
+  int L = 1;
+  for (int i = 0; i < s; ++i) { L *= P.rad[i]; P.len[i] = L; }
+  // the output slots a truncation keeps are [0, keep_half) and [n - keep_half, n)
+  P.prune_mid = (s > 0 && P.rad[s - 1] == 3 && keep_half > 0 && keep_half * 3 == n) ? 1 : 0;
   std::vector<int> perm(n);
   for (int f = 0; f < n; ++f) {
-    int pos = 0, x = f;
-    for (int i = 0; i < s; ++i) {
-      const int q = x % P.rad[i];
-      x /= P.rad[i];
-      pos += q * (P.len[i] / P.rad[i]);
+    int pos = 0, x = f, len = n;
+    for (int i = s - 1; i >= 0; --i) {
+      const int r = P.rad[i], sub = len / r;
+      pos += (x % r) * sub;
+      x /= r;
+      len = sub;
     }
     perm[f] = pos;
   }
@@ -194,10 +204,12 @@ size_t field_elems(const lh_handle* h, char grid) {
 int build_dt_tables(lh_handle* h) {
   const Dims& d = h->d;
   const int nyu = d.nyu, nyv = d.nyv, n0 = d.nn + 3;
-  std::vector<double> all(3 * 3 * nyu + 3 * 3 * nyv + 3 * n0);
+  const size_t np = d.np;
+  std::vector<double> all(3 * 3 * nyu + 3 * 3 * nyv + 3 * n0 + 3 * np);
   double* luu = all.data();
   double* luv = luu + 9 * nyu;
   double* u11 = luv + 9 * nyv;
+  double* iaxz = u11 + 3 * n0;
   for (int k = 0; k < 3; ++k) {
     const double beta = h->bRK[k] * h->dt / h->Re;
     for (int grid = 0; grid < 2; ++grid) {
@@ -247,6 +259,11 @@ int build_dt_tables(lh_handle* h) {
     double Q = 0.0;
     for (int j = 1; j <= nn + 1; ++j) Q = Q + (h->yv[j - ju0] - h->yv[j - 1 - ju0]) * x[j - 1];
     h->Qx1[k] = Q;
+    // 1/axz per column (LU_build, tridLU_3D_IB.f90:484-491)
+    for (size_t col = 0; col < np; ++col) {
+      const int i = (int)(col % d.nkx), kk = (int)(col / d.nkx);
+      iaxz[(size_t)k * np + col] = 1.0 / (1.0 - beta * (h->k2x[i] + h->k2z[kk]));
+    }
   }
   if (!h->tabs) {
     int rc = dalloc(h, &h->tabs, all.size());
@@ -256,6 +273,7 @@ int build_dt_tables(lh_handle* h) {
   h->t.lu_u = h->tabs;
   h->t.lu_v = h->tabs + 9 * nyu;
   h->t.u11 = h->tabs + 9 * nyu + 9 * nyv;
+  h->t.iaxz = h->tabs + 9 * nyu + 9 * nyv + 3 * n0;
   CU(h, cudaStreamSynchronize(h->st));
   return LH_OK;
 }
@@ -311,7 +329,7 @@ int enqueue_substage(lh_handle* h, int k, int upto) {
     a.tipu[0] = h->tipu[0]; a.tipu[1] = h->tipu[1]; a.tipv[0] = h->tipv[0]; a.tipv[1] = h->tipv[1];
     a.sc = h->sc;
     a.C1 = h->aRK[k] / h->Re; a.C2 = -h->cRK[k]; a.d = h->dRK[k]; a.g = h->gRK[k];
-    a.dt = h->dt; a.beta = beta;
+    a.dt = h->dt; a.beta = beta; a.k = k;
     launch_assemble(a, d, h->t, st);
     mark(h, K_ASSEMBLE);
   }
@@ -440,6 +458,10 @@ int host_flowrate(lh_handle* h, double* Q) {
 
 namespace lh {
 void set_init_error(const char* msg) { g_init_error = msg; }
+void set_handle_error(lh_handle* h, const char* msg) {
+  if (h) h->err = msg;
+  else g_init_error = msg;
+}
 }  // namespace lh
 
 extern "C" {
@@ -525,7 +547,7 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
   }
   int rc;
   // FFT plans: z of length ngz, x through a complex transform of ngx/2
-  if ((rc = build_plan(h, h->pz, d.ngz)) || (rc = build_plan(h, h->ph, d.ngx / 2))) return bail(rc);
+  if ((rc = build_plan(h, h->pz, d.ngz, d.nz / 2)) || (rc = build_plan(h, h->ph, d.ngx / 2, 0))) return bail(rc);
   {
     std::vector<double2> rt(d.ngx / 2 + 1);
     for (int k = 0; k <= d.ngx / 2; ++k) {
@@ -658,6 +680,26 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
     h->mixib = m;
     h->mixly = m + cb * (size_t)d.mp * nib;
     if ((rc = dalloc(h, &h->spec, (3 * (size_t)d.nyu + d.nyv + d.nyp) * d.np))) return bail(rc);
+    if ((rc = dalloc(h, &h->stat, 13 * (size_t)std::max(d.nyu, d.nyv)))) return bail(rc);
+    if (prm->geometry_type == 3) {
+      if (prm->ntilex <= 0 || prm->ntilez <= 0 || d.ngx % prm->ntilex || d.ngz % prm->ntilez)
+        return bail(fail(h, LH_EINVAL, "ntilex/ntilez must be positive and divide Ngalx/Ngalz"));
+      h->dnx = d.ngx / prm->ntilex;
+      h->dnz = d.ngz / prm->ntilez;
+      h->nju = Nf(4, 1) - Nf(4, 0) + 1;
+      h->njv = Nf(3, 1) - Nf(3, 0) + 1;
+      h->njp = Nf(4, 1) - Nf(4, 0) - 1;
+      if (h->nju < 1 || h->njv < 1 || h->njp < 1 || 2 * h->nju > d.nyu || 2 * h->njv > d.nyv || 2 * h->njp > d.nyp)
+        return bail(fail(h, LH_EINVAL, "wall bands inconsistent with the y grid"));
+      std::vector<int> ul(2 * h->nju), vl(2 * h->njv), pl(2 * h->njp);
+      for (int j = 0; j < h->nju; ++j) { ul[2 * j] = j; ul[2 * j + 1] = d.nyu - 1 - j; }
+      for (int j = 0; j < h->njv; ++j) { vl[2 * j] = j; vl[2 * j + 1] = d.nyv - 1 - j; }
+      for (int j = 0; j < h->njp; ++j) { pl[2 * j] = j; pl[2 * j + 1] = d.nyp - 1 - j; }
+      const size_t tile = (size_t)h->dnx * h->dnz;
+      if ((rc = upload(h, &h->cond_ul, ul)) || (rc = upload(h, &h->cond_vl, vl)) || (rc = upload(h, &h->cond_pl, pl)) ||
+          (rc = dalloc(h, &h->cond, tile * (6 * (size_t)h->nju + 3 * (size_t)h->njv + 2 * (size_t)h->njp))))
+        return bail(rc);
+    }
   }
   // launch shapes: z tile width and levels per x-pass chunk
   // z tile width: narrow tiles keep several CTAs per SM so that one CTA's loads overlap another's
@@ -982,11 +1024,92 @@ int lh_spectra_flush(lh_handle* h, double* spU, double* spV, double* spW, double
 }
 
 int lh_stats_accumulate(lh_handle* h) {
-  return h ? fail(h, LH_EUNSUPPORTED, "plane statistics are not built yet") : LH_EINVAL;
+  if (!h) return LH_EINVAL;
+  if (!h->have_fields) return fail(h, LH_ESTATE, "fields must be set first");
+  cudaSetDevice(h->device);
+  // v at centres and w at faces are staged in the right-hand-side buffers, which are dead between steps
+  launch_stats(h->u1, h->u2, h->u3, h->p, h->r1, h->r3, h->stat, h->d, h->t, h->st);
+  CU(h, cudaGetLastError());
+  h->nstat += 1;
+  return LH_OK;
 }
 
-int lh_stats_flush(lh_handle* h, double*, int32_t*, int32_t) {
-  return h ? fail(h, LH_EUNSUPPORTED, "plane statistics are not built yet") : LH_EINVAL;
+int lh_cond_accumulate(lh_handle* h) {
+  if (!h) return LH_EINVAL;
+  if (!h->have_fields) return fail(h, LH_ESTATE, "fields must be set first");
+  if (!h->cond) return LH_OK;  // no canopies: nothing to accumulate
+  cudaSetDevice(h->device);
+  const Dims& d = h->d;
+  cudaStream_t st = h->st;
+  // v at centres and w at faces staged in the right-hand-side scratch (dead between steps)
+  launch_stage_itp(h->u2, h->u3, h->r1, h->r3, d, h->t, st);
+  // the FP64 mixed planes of one chunk live in the substage's mixed buffers: 2 planes (both walls) per j1
+  const size_t cb = h->precision == LH_PREC_MIXED ? sizeof(float2) : sizeof(double2);
+  const int cap = (int)((size_t)d.nyu * cb / (2 * sizeof(double2)));
+  if (cap < 1) return fail(h, LH_EINVAL, "no room for the conditional statistics planes");
+  const size_t tile = (size_t)h->dnx * h->dnz;
+  const int njmax = std::max(h->nju, std::max(h->njv, h->njp));
+  double2* mx[6] = {(double2*)h->mixu, (double2*)h->mixw, (double2*)h->mixp[0], (double2*)h->mixp[1],
+                    (double2*)h->mixp[2], (double2*)h->mixp[3]};
+  for (int j0 = 0; j0 < njmax; j0 += cap) {
+    const int cu = std::max(0, std::min(cap, h->nju - j0)), cvv = std::max(0, std::min(cap, h->njv - j0)),
+              cp = std::max(0, std::min(cap, h->njp - j0));
+    ZJobs<double> J{};
+    J.j[0] = ZJob<double>{h->u1, nullptr, mx[0], h->cond_ul + 2 * j0, 0, 2 * cu};
+    J.j[1] = ZJob<double>{h->u3, nullptr, mx[1], h->cond_ul + 2 * j0, 0, 2 * cu};
+    J.j[2] = ZJob<double>{h->r1, nullptr, mx[2], h->cond_ul + 2 * j0, 0, 2 * cu};
+    J.j[3] = ZJob<double>{h->u2, nullptr, mx[3], h->cond_vl + 2 * j0, 0, 2 * cvv};
+    J.j[4] = ZJob<double>{h->r3, nullptr, mx[4], h->cond_vl + 2 * j0, 0, 2 * cvv};
+    J.j[5] = ZJob<double>{h->p, nullptr, mx[5], h->cond_pl + 2 * j0, 0, 2 * cp};
+    J.njobs = 6;
+    J.maxlev = 2 * std::max(cu, std::max(cvv, cp));
+    launch_zinv<double>(J, d, h->pz.plan, h->tx, st);
+    CondArgs a{};
+    a.mix[0][0] = mx[0]; a.mix[0][1] = mx[1]; a.mix[0][2] = mx[2];
+    a.mix[1][0] = mx[3]; a.mix[1][1] = mx[4];
+    a.mix[2][0] = mx[5];
+    a.out[0] = h->cond;
+    a.out[1] = h->cond + 6 * (size_t)h->nju * tile;
+    a.out[2] = a.out[1] + 3 * (size_t)h->njv * tile;
+    a.nj[0] = cu; a.nj[1] = cvv; a.nj[2] = cp;
+    a.njtot[0] = h->nju; a.njtot[1] = h->njv; a.njtot[2] = h->njp;
+    a.j0 = j0;
+    a.dnx = h->dnx; a.dnz = h->dnz; a.ntx = d.ngx / h->dnx; a.ntz = d.ngz / h->dnz;
+    launch_xcond(a, d, h->ph.plan, h->rtw, st);
+  }
+  CU(h, cudaGetLastError());
+  h->ncond += 1;
+  return LH_OK;
+}
+
+int lh_cond_flush(lh_handle* h, double* out, int32_t* dims, int32_t* count, int32_t reset) {
+  if (!h) return LH_EINVAL;
+  cudaSetDevice(h->device);
+  if (dims) { dims[0] = h->nju; dims[1] = h->njv; dims[2] = h->njp; dims[3] = h->dnx; dims[4] = h->dnz; }
+  if (count) *count = h->ncond;
+  if (!h->cond) return LH_OK;
+  const size_t n = (size_t)h->dnx * h->dnz * (6 * (size_t)h->nju + 3 * (size_t)h->njv + 2 * (size_t)h->njp);
+  if (out) CU(h, cudaMemcpyAsync(out, h->cond, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  if (reset) {
+    CU(h, cudaMemsetAsync(h->cond, 0, n * sizeof(double), h->st));
+    h->ncond = 0;
+  }
+  CU(h, cudaStreamSynchronize(h->st));
+  return LH_OK;
+}
+
+int lh_stats_flush(lh_handle* h, double* out, int32_t* count, int32_t reset) {
+  if (!h) return LH_EINVAL;
+  cudaSetDevice(h->device);
+  const size_t n = 13 * (size_t)std::max(h->d.nyu, h->d.nyv);
+  if (out) CU(h, cudaMemcpyAsync(out, h->stat, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  if (count) *count = h->nstat;
+  if (reset) {
+    CU(h, cudaMemsetAsync(h->stat, 0, n * sizeof(double), h->st));
+    h->nstat = 0;
+  }
+  CU(h, cudaStreamSynchronize(h->st));
+  return LH_OK;
 }
 
 }  // extern "C"

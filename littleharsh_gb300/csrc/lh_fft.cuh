@@ -1,12 +1,19 @@
-// lh_fft.cuh -- batched mixed-radix (4, 3, 2) FFTs in shared memory.
+// lh_fft.cuh -- batched mixed-radix (4, 2, 3) FFTs in shared memory.
 //
 // Replaces the FFTPACK-derived rfft/cfft kernels of the reference
 // (rft_buff.f, cft_buff.f).  Every transform is an in-place decimation-in-
-// frequency pass sequence over a batch of vectors held in shared memory; all
-// threads of the CTA share the butterflies of a stage.  The output of a DIF
-// sequence is in digit-reversed order; `perm[k]` gives the position of
-// frequency (or sample) k.  Twiddles are tables of exp(-2 pi i k / n)
-// computed on the host in extended precision, never evaluated on the device.
+// time pass sequence over a batch of vectors held in shared memory; all
+// threads of the CTA share the butterflies of a stage.  The input of a DIT
+// sequence sits at digit-reversed positions (`perm[n]` is where sample n is
+// stored) and the output comes out in natural order.  Twiddles are tables of
+// exp(-2 pi i k / n) computed on the host in extended precision, never
+// evaluated on the device.
+//
+// The butterflies are written for the FP64 pipe, which is the bottleneck on
+// GB300 (1.2 TFLOP/s): each twiddle multiplication is fused into the
+// butterfly's additions (a + w*c as two FMAs per component, a - w*c as
+// 2a - (a + w*c)), so a radix-4 butterfly costs 24 FP64 instructions instead
+// of 28, a radix-3 one 18 instead of 22 and a radix-2 one 6 instead of 8.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -22,10 +29,11 @@ constexpr int kMaxStages = 16;
 // One transform length.  Passed by value to kernels.
 struct FftPlan {
   int n;                  // length
-  int ns;                 // number of DIF stages
-  int rad[kMaxStages];    // radix of stage s
-  int len[kMaxStages];    // sub-transform length entering stage s (len[0] = n)
-  const int* perm;        // device: position of index k after the DIF stages
+  int ns;                 // number of DIT stages
+  int rad[kMaxStages];    // radix of stage s (radix 4 first: stage 0 needs no twiddles; radix 3 last)
+  int len[kMaxStages];    // transform length produced by stage s (len[ns-1] = n)
+  int prune_mid;          // last stage is radix 3 over n/3 and the middle third of the output is not needed
+  const int* perm;        // device: position of sample n at the start (digit reversal)
   const double2* tw64;    // device: exp(-2 pi i k/n), k = 0..n-1
   const float2* tw32;     // same, rounded to float
 };
@@ -36,16 +44,92 @@ template <> __device__ __forceinline__ const float2* twtab<float>(const FftPlan&
 
 template <typename T2> __device__ __forceinline__ T2 cadd(T2 a, T2 b) { return T2{a.x + b.x, a.y + b.y}; }
 template <typename T2> __device__ __forceinline__ T2 csub(T2 a, T2 b) { return T2{a.x - b.x, a.y - b.y}; }
-// a * w (SIGN < 0) or a * conj(w) (SIGN > 0), w from a table of exp(-i t)
-template <int SIGN, typename T2> __device__ __forceinline__ T2 ctw(T2 a, T2 w) {
-  if (SIGN < 0) return T2{a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x};
-  return T2{a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y};
+
+// b*w (SIGN < 0) or b*conj(w) (SIGN > 0), w from a table of exp(-i t): 2 instructions per component
+template <int SIGN, typename T2> __device__ __forceinline__ T2 cmul(T2 b, T2 w) {
+  if (SIGN < 0) return T2{fma(b.x, w.x, -(b.y * w.y)), fma(b.x, w.y, b.y * w.x)};
+  return T2{fma(b.x, w.x, b.y * w.y), fma(b.y, w.x, -(b.x * w.y))};
+}
+// a + b*w (or a + b*conj(w)): two FMAs per component
+template <int SIGN, typename T2> __device__ __forceinline__ T2 cmad(T2 a, T2 b, T2 w) {
+  if (SIGN < 0) return T2{fma(b.x, w.x, fma(-b.y, w.y, a.x)), fma(b.x, w.y, fma(b.y, w.x, a.y))};
+  return T2{fma(b.x, w.x, fma(b.y, w.y, a.x)), fma(b.y, w.x, fma(-b.x, w.y, a.y))};
+}
+// 2a - s: one FMA per component (the difference partner of s = a + x)
+template <typename T2> __device__ __forceinline__ T2 ctwice_minus(T2 a, T2 s) {
+  using R = decltype(a.x);
+  return T2{fma((R)2, a.x, -s.x), fma((R)2, a.y, -s.y)};
+}
+// SIGN*i*t
+template <int SIGN, typename T2> __device__ __forceinline__ T2 cimul(T2 t) {
+  return (SIGN < 0) ? T2{t.y, -t.x} : T2{-t.y, t.x};
 }
 
-// In-place DIF over `nb` vectors: element e of vector b at buf[b*bs + e*es].
-// SIGN = -1 forward (exp(-i)), +1 inverse (exp(+i)); no normalisation.
+// One DIT butterfly of radix r at `base` (elements base[p*st], p = 0..r-1),
+// twiddle exponent step e = k*(n/L) (0 for the first stage).
 template <typename R, int SIGN>
-__device__ void fft_dif(cpx_t<R>* buf, int nb, int es, int bs, const FftPlan& P) {
+__device__ __forceinline__ void dit_butterfly(cpx_t<R>* base, int st, int r, int e, bool twiddle, bool skip_mid,
+                                              const cpx_t<R>* __restrict__ tw) {
+  using T2 = cpx_t<R>;
+  if (r == 4) {
+    const T2 a = base[0], b = base[st], c = base[2 * st], d = base[3 * st];
+    T2 t0, t1, t2, t3;
+    if (twiddle) {
+      const T2 w1 = tw[e], w2 = tw[2 * e], w3 = tw[3 * e];
+      t0 = cmad<SIGN>(a, c, w2);
+      t1 = ctwice_minus(a, t0);
+      const T2 B = cmul<SIGN>(b, w1);
+      t2 = cmad<SIGN>(B, d, w3);
+      t3 = ctwice_minus(B, t2);
+    } else {
+      t0 = cadd(a, c); t1 = csub(a, c); t2 = cadd(b, d); t3 = csub(b, d);
+    }
+    const T2 u = cimul<SIGN>(t3);
+    base[0] = cadd(t0, t2);
+    base[st] = cadd(t1, u);
+    base[2 * st] = csub(t0, t2);
+    base[3 * st] = csub(t1, u);
+  } else if (r == 2) {
+    const T2 a = base[0], b = base[st];
+    if (twiddle) {
+      const T2 s = cmad<SIGN>(a, b, tw[e]);
+      base[0] = s;
+      base[st] = ctwice_minus(a, s);
+    } else {
+      base[0] = cadd(a, b);
+      base[st] = csub(a, b);
+    }
+  } else {  // r == 3: X1 = a - t1/2 + SIGN*i*(sqrt3/2)(B - C), X2 its mirror
+    const R s3 = (SIGN < 0) ? (R)-0.86602540378443864676 : (R)0.86602540378443864676;
+    const T2 a = base[0], b = base[st], c = base[2 * st];
+    T2 t1, d;
+    if (twiddle) {
+      const T2 B = cmul<SIGN>(b, tw[e]);
+      t1 = cmad<SIGN>(B, c, tw[2 * e]);
+      d = ctwice_minus(B, t1);
+    } else {
+      t1 = cadd(b, c);
+      d = csub(b, c);
+    }
+    const T2 t2 = T2{fma((R)-0.5, t1.x, a.x), fma((R)-0.5, t1.y, a.y)};
+    base[0] = cadd(a, t1);
+    if (skip_mid) {
+      base[2 * st] = T2{fma(s3, d.y, t2.x), fma(-s3, d.x, t2.y)};
+    } else {
+      const T2 x1 = T2{fma(-s3, d.y, t2.x), fma(s3, d.x, t2.y)};
+      base[st] = x1;
+      base[2 * st] = ctwice_minus(t2, x1);
+    }
+  }
+}
+
+// In-place DIT over `nb` vectors: element e of vector b at buf[b*bs + e*es].
+// BFAST: consecutive threads take consecutive vectors (for interleaved
+// vectors, es = nb-ish, bs = 1); otherwise consecutive butterflies of one
+// vector (es = 1).  SIGN = -1 forward, +1 inverse; no normalisation.
+// prune: skip the middle output third of the last radix-3 stage.
+template <typename R, int SIGN, bool BFAST>
+__device__ void fft_dit(cpx_t<R>* buf, int nb, int es, int bs, const FftPlan& P, bool prune) {
   using T2 = cpx_t<R>;
   const T2* __restrict__ tw = twtab<R>(P);
   const int n = P.n;
@@ -53,42 +137,15 @@ __device__ void fft_dif(cpx_t<R>* buf, int nb, int es, int bs, const FftPlan& P)
     const int r = P.rad[s], L = P.len[s], m = L / r, ts = n / L;
     const int nbf = n / r;
     const int total = nb * nbf;
+    const bool twiddle = m > 1;
+    const bool skip_mid = prune && s == P.ns - 1;
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      const int b = t / nbf, f = t - b * nbf;
+      int b, f;
+      if (BFAST) { f = t / nb; b = t - f * nb; }
+      else { b = t / nbf; f = t - b * nbf; }
       const int blk = f / m, k = f - blk * m;
       T2* base = buf + b * bs + (blk * L + k) * es;
-      const int st = m * es;
-      if (r == 4) {
-        T2 a = base[0], bb = base[st], c = base[2 * st], d = base[3 * st];
-        T2 t0 = cadd(a, c), t1 = csub(a, c), t2 = cadd(bb, d), t3 = csub(bb, d);
-        // SIGN*i*t3
-        T2 u = (SIGN < 0) ? T2{t3.y, -t3.x} : T2{-t3.y, t3.x};
-        T2 y0 = cadd(t0, t2), y2 = csub(t0, t2), y1 = cadd(t1, u), y3 = csub(t1, u);
-        if (m > 1) {
-          y1 = ctw<SIGN>(y1, tw[k * ts]);
-          y2 = ctw<SIGN>(y2, tw[2 * k * ts]);
-          y3 = ctw<SIGN>(y3, tw[3 * k * ts]);
-        }
-        base[0] = y0; base[st] = y1; base[2 * st] = y2; base[3 * st] = y3;
-      } else if (r == 2) {
-        T2 a = base[0], bb = base[st];
-        T2 y0 = cadd(a, bb), y1 = csub(a, bb);
-        if (m > 1) y1 = ctw<SIGN>(y1, tw[k * ts]);
-        base[0] = y0; base[st] = y1;
-      } else {  // r == 3
-        const R h = (R)0.5;
-        const R s3 = (SIGN < 0) ? (R)-0.86602540378443864676 : (R)0.86602540378443864676;
-        T2 a = base[0], bb = base[st], c = base[2 * st];
-        T2 t1 = cadd(bb, c), d = csub(bb, c);
-        T2 t2 = T2{a.x - h * t1.x, a.y - h * t1.y};
-        T2 u = T2{-s3 * d.y, s3 * d.x};  // i*s3*d
-        T2 y0 = cadd(a, t1), y1 = cadd(t2, u), y2 = csub(t2, u);
-        if (m > 1) {
-          y1 = ctw<SIGN>(y1, tw[k * ts]);
-          y2 = ctw<SIGN>(y2, tw[2 * k * ts]);
-        }
-        base[0] = y0; base[st] = y1; base[2 * st] = y2;
-      }
+      dit_butterfly<R, SIGN>(base, m * es, r, k * ts, twiddle, skip_mid, tw);
     }
     __syncthreads();
   }

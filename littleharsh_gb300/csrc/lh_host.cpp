@@ -280,6 +280,8 @@ extern "C" int lh_setup_grid(const lh_input* in, lh_params* prm, double* yu_o, d
   prm->dsty = in->dsty;
   prm->Re = in->Re; prm->alp = in->alp; prm->bet = in->bet;
   prm->ddthetavi = 1.0;
+  prm->ntilex = in->ntilex;
+  prm->ntilez = in->ntilez;
   for (int c = 0; c < 2; ++c)
     for (int b = 0; b < 3; ++b) prm->gridweighting[c * 3 + b] = gw[b][c];
   if (yu_o) std::memcpy(yu_o, yu.data(), sizeof(double) * nyu);

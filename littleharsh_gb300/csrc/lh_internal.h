@@ -36,6 +36,7 @@ struct Tables {
   const double* lu_u;  // [3 kRK][3][nyu] Helmholtz LU (a1, 1/diag, scaled a3), u grid
   const double* lu_v;  // [3 kRK][3][nyv] same, v grid
   const double* u11;   // [3 kRK][nn+3] unit-gradient response of mode (0,0)
+  const double* iaxz;  // [3 kRK][np] 1/axz = 1/(1 - beta_k (k2x + k2z)) per column
   const double* dg1;   // [nyp] pressure LU lower diagonal (column independent)
   const double* dg2;   // [nyp][np] pressure LU 1/diag per column
   const double* dg3;   // [nyp][np] pressure LU scaled upper diagonal per column
@@ -120,6 +121,7 @@ struct AsmArgs {
   int tipu[2], tipv[2];      // level indices of the tip planes (u grid, v grid) or -1
   const DevScalars* sc;
   double C1, C2, d, g, dt, beta;
+  int k;                     // substage index 0..2 (selects 1/axz)
 };
 void launch_assemble(const AsmArgs& a, const Dims& d, const Tables& t, cudaStream_t st);
 
@@ -136,6 +138,20 @@ void launch_absmax(const double2* x, size_t n, DevScalars* sc, cudaStream_t st);
 void launch_transpose(const double2* src, double2* dst, int rows, int cols, cudaStream_t st);
 void launch_spectra(const double2* u1, const double2* u2, const double2* u3, const double2* p, double* sp,
                     const Dims& d, const Tables& t, cudaStream_t st);
+void launch_stats(const double2* u1, const double2* u2, const double2* u3, const double2* p, double2* vc,
+                  double2* wf, double* acc, const Dims& d, const Tables& t, cudaStream_t st);
+// Conditional statistics pass over one chunk of wall-band planes (grids g: 0 u, 1 v, 2 p).
+struct CondArgs {
+  const double2* mix[3][3];  // mixed planes per grid and field (u: u, w, v at centres; v: v, w at faces; p: p)
+  double* out[3];            // accumulators per grid: [quantity][j1][kin][i]
+  int nj[3];                 // planes of this chunk per grid
+  int njtot[3];              // planes per grid in total
+  int j0;                    // first j1 of the chunk
+  int dnx, dnz, ntx, ntz;
+};
+void launch_stage_itp(const double2* u2, const double2* u3, double2* vc, double2* wf, const Dims& d, const Tables& t,
+                      cudaStream_t st);
+void launch_xcond(const CondArgs& a, const Dims& d, const FftPlan& ph, const double2* rtw, cudaStream_t st);
 cudaError_t configure_kernels();
 
 // Message returned by lh_last_error(NULL) on this thread (lh_capi.cu).

@@ -33,57 +33,6 @@ namespace lh {
 // z passes
 // ---------------------------------------------------------------------------
 
-// Batch-fast DIF: consecutive threads take consecutive vectors of the batch,
-// so a warp touches contiguous shared memory when vectors are interleaved.
-template <typename R, int SIGN>
-__device__ void fft_dif_bfast(cpx_t<R>* buf, int nb, int es, const FftPlan& P) {
-  using T2 = cpx_t<R>;
-  const T2* __restrict__ tw = twtab<R>(P);
-  const int n = P.n;
-  for (int s = 0; s < P.ns; ++s) {
-    const int r = P.rad[s], L = P.len[s], m = L / r, ts = n / L;
-    const int nbf = n / r;
-    const int total = nb * nbf;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      const int f = t / nb, b = t - f * nb;
-      const int blk = f / m, k = f - blk * m;
-      T2* base = buf + b + (blk * L + k) * es;
-      const int st = m * es;
-      if (r == 4) {
-        T2 a = base[0], bb = base[st], c = base[2 * st], d = base[3 * st];
-        T2 t0 = cadd(a, c), t1 = csub(a, c), t2 = cadd(bb, d), t3 = csub(bb, d);
-        T2 u = (SIGN < 0) ? T2{t3.y, -t3.x} : T2{-t3.y, t3.x};
-        T2 y0 = cadd(t0, t2), y2 = csub(t0, t2), y1 = cadd(t1, u), y3 = csub(t1, u);
-        if (m > 1) {
-          y1 = ctw<SIGN>(y1, tw[k * ts]);
-          y2 = ctw<SIGN>(y2, tw[2 * k * ts]);
-          y3 = ctw<SIGN>(y3, tw[3 * k * ts]);
-        }
-        base[0] = y0; base[st] = y1; base[2 * st] = y2; base[3 * st] = y3;
-      } else if (r == 2) {
-        T2 a = base[0], bb = base[st];
-        T2 y0 = cadd(a, bb), y1 = csub(a, bb);
-        if (m > 1) y1 = ctw<SIGN>(y1, tw[k * ts]);
-        base[0] = y0; base[st] = y1;
-      } else {
-        const R h = (R)0.5;
-        const R s3 = (SIGN < 0) ? (R)-0.86602540378443864676 : (R)0.86602540378443864676;
-        T2 a = base[0], bb = base[st], c = base[2 * st];
-        T2 t1 = cadd(bb, c), d = csub(bb, c);
-        T2 t2 = T2{a.x - h * t1.x, a.y - h * t1.y};
-        T2 u = T2{-s3 * d.y, s3 * d.x};
-        T2 y0 = cadd(a, t1), y1 = cadd(t2, u), y2 = csub(t2, u);
-        if (m > 1) {
-          y1 = ctw<SIGN>(y1, tw[k * ts]);
-          y2 = ctw<SIGN>(y2, tw[2 * k * ts]);
-        }
-        base[0] = y0; base[st] = y1; base[2 * st] = y2;
-      }
-    }
-    __syncthreads();
-  }
-}
-
 template <typename R>
 __global__ void __launch_bounds__(256) k_zinv(ZJobs<R> jobs, Dims d, FftPlan pz, int tx) {
   using T2 = cpx_t<R>;
@@ -98,7 +47,8 @@ __global__ void __launch_bounds__(256) k_zinv(ZJobs<R> jobs, Dims d, FftPlan pz,
   const int nb = min(tx, d.nkx - i0);
   const double2* __restrict__ src = J.spec_in + (size_t)lev * d.np;
   const int h = d.nz / 2, gap = d.ngz - d.nz;
-  for (int e = threadIdx.x; e < gap * tx; e += blockDim.x) sm[(h + e / tx) * tx + (e % tx)] = T2{0, 0};
+  // samples go to their digit-reversed positions; the 3/2 padding slots are zero
+  for (int e = threadIdx.x; e < gap * tx; e += blockDim.x) sm[pz.perm[h + e / tx] * tx + (e % tx)] = T2{0, 0};
   for (int e = threadIdx.x; e < d.nz * tx; e += blockDim.x) {
     const int kk = e / tx, c = e - kk * tx;
     const int slot = kk < h ? kk : kk + gap;
@@ -107,14 +57,14 @@ __global__ void __launch_bounds__(256) k_zinv(ZJobs<R> jobs, Dims d, FftPlan pz,
       const double2 s = src[(size_t)kk * d.nkx + i0 + c];
       v = T2{(R)s.x, (R)s.y};
     }
-    sm[slot * tx + c] = v;
+    sm[pz.perm[slot] * tx + c] = v;
   }
   __syncthreads();
-  fft_dif_bfast<R, +1>(sm, nb, tx, pz);
+  fft_dit<R, +1, true>(sm, nb, tx, 1, pz, false);
   T2* __restrict__ dst = J.mix + (size_t)y * d.mp;
   for (int e = threadIdx.x; e < d.ngz * tx; e += blockDim.x) {
     const int z = e / tx, c = e - z * tx;
-    if (c < nb) dst[(size_t)z * d.nkx + i0 + c] = sm[pz.perm[z] * tx + c];
+    if (c < nb) dst[(size_t)z * d.nkx + i0 + c] = sm[z * tx + c];
   }
 }
 
@@ -133,17 +83,19 @@ __global__ void __launch_bounds__(256) k_zfwd(ZJobs<R> jobs, Dims d, FftPlan pz,
   const T2* __restrict__ src = J.mix + (size_t)y * d.mp;
   for (int e = threadIdx.x; e < d.ngz * tx; e += blockDim.x) {
     const int z = e / tx, c = e - z * tx;
-    sm[z * tx + c] = (c < nb) ? src[(size_t)z * d.nkx + i0 + c] : T2{0, 0};
+    sm[pz.perm[z] * tx + c] = (c < nb) ? src[(size_t)z * d.nkx + i0 + c] : T2{0, 0};
   }
   __syncthreads();
-  fft_dif_bfast<R, -1>(sm, nb, tx, pz);
+  // the truncation keeps slots [0, N2/2) and [Ngz - N2/2, Ngz): the middle third of the last radix-3
+  // stage's output is never read when N2/2 = Ngz/3
+  fft_dit<R, -1, true>(sm, nb, tx, 1, pz, pz.prune_mid != 0);
   double2* __restrict__ dst = J.spec_out + (size_t)lev * d.np;
   const int h = d.nz / 2, gap = d.ngz - d.nz;
   for (int e = threadIdx.x; e < d.nz * tx; e += blockDim.x) {
     const int kk = e / tx, c = e - kk * tx;
     if (c < nb) {
       const int slot = kk < h ? kk : kk + gap;
-      const T2 v = sm[pz.perm[slot] * tx + c];
+      const T2 v = sm[slot * tx + c];
       dst[(size_t)kk * d.nkx + i0 + c] = double2{(double)v.x * scale, (double)v.y * scale};
     }
   }
@@ -188,13 +140,13 @@ __device__ void x_inverse(const cpx_t<R>* const* rows, int nr, cpx_t<R>* F, int 
     const double2 w = rtw[k];
     const R wr = (R)w.x, wi = (R)-w.y;  // exp(+2 pi i k/n)
     const T2 q = T2{wr * df.x - wi * df.y, wr * df.y + wi * df.x};
-    F[r * hp + k] = T2{s.x - q.y, s.y + q.x};
+    F[r * hp + ph.perm[k]] = T2{s.x - q.y, s.y + q.x};
   }
   __syncthreads();
-  fft_dif<R, +1>(F, nr, 1, hp, ph);
+  fft_dit<R, +1, false>(F, nr, 1, hp, ph, false);
   for (int e = threadIdx.x; e < nr * h; e += blockDim.x) {
     const int r = e / h, m = e - r * h;
-    const T2 z = F[r * hp + ph.perm[m]];
+    const T2 z = F[r * hp + m];
     out[r][2 * m] = z.x;
     out[r][2 * m + 1] = z.y;
   }
@@ -202,19 +154,20 @@ __device__ void x_inverse(const cpx_t<R>* const* rows, int nr, cpx_t<R>* F, int 
 }
 
 // Forward real transform of the data already packed in F (z[m] = x[2m] + i
-// x[2m+1], natural order) into nr mixed rows scaled by 1/ngx, kx < nkx kept.
+// x[2m+1] stored at position perm[m]) into nr mixed rows scaled by 1/ngx,
+// kx < nkx kept.
 template <typename R>
 __device__ void x_forward_packed(int nr, cpx_t<R>* F, int hp, cpx_t<R>* const* rows, const Dims& d,
                                  const FftPlan& ph, const double2* __restrict__ rtw) {
   using T2 = cpx_t<R>;
   const int h = d.ngx / 2, nkx = d.nkx;
   const R scale = (R)(1.0 / d.ngx);
-  fft_dif<R, -1>(F, nr, 1, hp, ph);
+  fft_dit<R, -1, false>(F, nr, 1, hp, ph, false);
   for (int e = threadIdx.x; e < nr * nkx; e += blockDim.x) {
     const int r = e / nkx, k = e - r * nkx;
-    const T2 zk = F[r * hp + ph.perm[k]];
+    const T2 zk = F[r * hp + k];
     const int k2 = (h - k) % h;
-    T2 zc = F[r * hp + ph.perm[k2]];
+    T2 zc = F[r * hp + k2];
     zc.y = -zc.y;
     const T2 E = T2{(R)0.5 * (zk.x + zc.x), (R)0.5 * (zk.y + zc.y)};
     const T2 D = csub(zk, zc);
@@ -295,9 +248,10 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
           cmax = fmax(cmax, cv);
         }
       }
+      const int pm = ph.perm[m];
 #pragma unroll
       for (int r = 0; r < 6; ++r)
-        if (r < 4 || fprod) F[r * hp + m] = T2{q[r][0], q[r][1]};
+        if (r < 4 || fprod) F[r * hp + pm] = T2{q[r][0], q[r][1]};
     }
     __syncthreads();
     {
@@ -365,7 +319,7 @@ __global__ void __launch_bounds__(128) k_xmask(MaskArgs<R> a, Dims d, FftPlan ph
       v[e] = rr[x];
       if (msk[x]) v[e] = (tip >= 0) ? mb * ll[x] : (R)0;
     }
-    F[m] = T2{v[0], v[1]};
+    F[ph.perm[m]] = T2{v[0], v[1]};
   }
   __syncthreads();
   T2* rows[1] = {row};
@@ -395,7 +349,9 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
   const int np = d.np;
   const int i = col % d.nkx, kk = col / d.nkx;
   const double kx = t.kx[i], kz = t.kz[kk], k2 = t.k2x[i] + t.k2z[kk];
-  const double axz = 1.0 - a.beta * (t.k2x[i] + t.k2z[kk]);
+  // 1/axz of LUsolU/LUsolV (tridLU_3D_IB.f90:489,93) for this substage: a multiply instead of a
+  // division, which costs ~10 FP64 instructions on a part with little FP64 throughput
+  const double iaxz = t.iaxz[(size_t)a.k * np + col];
   const size_t c0 = (size_t)jj * np + col;
   // u1 and u3 on centre jj
   if (jj == 0 || jj == d.nyu - 1) {
@@ -428,7 +384,7 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
       (f == 0 ? a.n1 : a.n3)[c0] = double2{nr, ni};
       rx = rx - a.g * nr;
       ry = ry - a.g * ni;
-      (f == 0 ? a.r1 : a.r3)[c0] = double2{(u0.x + a.dt * rx) / axz, (u0.y + a.dt * ry) / axz};
+      (f == 0 ? a.r1 : a.r3)[c0] = double2{(u0.x + a.dt * rx) * iaxz, (u0.y + a.dt * ry) * iaxz};
       if (tip) {
         const double ly_x = a1 * um.x + (a2)*u0.x + a3 * up.x;
         const double ly_y = a1 * um.y + (a2)*u0.y + a3 * up.y;
@@ -458,7 +414,7 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
       a.n2[c0] = double2{nr, ni};
       rx = rx - a.g * nr;
       ry = ry - a.g * ni;
-      a.r2[c0] = double2{(u0.x + a.dt * rx) / axz, (u0.y + a.dt * ry) / axz};
+      a.r2[c0] = double2{(u0.x + a.dt * rx) * iaxz, (u0.y + a.dt * ry) * iaxz};
       if (jj == a.tipv[0] || jj == a.tipv[1]) {
         const int tslot = (jj == a.tipv[0]) ? 0 : 1;
         a.lytip[(size_t)(4 + tslot) * np + col] =
@@ -749,6 +705,198 @@ __global__ void k_spectra(const double2* u1, const double2* u2, const double2* u
   }
 }
 
+// Plane statistics of stats.f90:1-108 (sums over the physical plane of each
+// level), accumulated without transforms: the physical plane is the exact
+// inverse DFT of the zero-padded spectrum, so by Parseval
+//   sum_{x,z} f g = Ngx Ngz [ sum_{kx>0} 2 Re(f g*) + sum_kz h_f h_g* ],
+// where h is the kx = 0 line made Hermitian the way the real x-inverse
+// makes it (its imaginary part is dropped; the lone kz = -N2/2 mode splits
+// into -N2/2 and +N2/2 on the padded grid).  sum f = Ngx Ngz Re f(0,0).
+// acc rows (length L = max(nyu, nyv)): 0 Um 1 U2m 2 Vm 3 V2m 4 Wm 5 W2m 6 Pm 7 P2m
+// 8 UVm (u, v at centres) 9 UWm 10 VWm (v, w at faces).  One block per level.
+__device__ __forceinline__ double pair_term(const double2* f, const double2* g, int col, int i, int kk, int nz,
+                                            int nkx) {
+  const double2 a = f[col], b = g[col];
+  const double re = a.x * b.x + a.y * b.y;  // Re(a conj b)
+  if (i > 0) return 2.0 * re;
+  if (kk == nz / 2) return 0.5 * re;
+  const int pk = (nz - kk) % nz;
+  const double2 c = g[(size_t)pk * nkx];
+  return 0.5 * (re + (a.x * c.x - a.y * c.y));  // + Re(a g(-kz))
+}
+
+__global__ void __launch_bounds__(256) k_stats(const double2* u1, const double2* u2, const double2* u3,
+                                               const double2* p, double2* vc, double2* wf, double* acc, Dims d,
+                                               Tables t, int L) {
+  const int jj = blockIdx.x;
+  const size_t np = d.np;
+  double s[11];
+#pragma unroll
+  for (int r = 0; r < 11; ++r) s[r] = 0.0;
+  // v at the centre jj and w at the face jj (zero on ghost centres and wall faces)
+  double2* vcl = vc + (size_t)blockIdx.x * np;
+  double2* wfl = wf + (size_t)blockIdx.x * np;
+  const bool cin = jj >= 1 && jj <= d.nyu - 2, fin = jj >= 1 && jj <= d.nyv - 2;
+  for (int col = threadIdx.x; col < d.np; col += blockDim.x) {
+    double2 v = double2{0.0, 0.0}, w = double2{0.0, 0.0};
+    if (cin) {
+      const double2 v0 = u2[(size_t)(jj - 1) * np + col], v1 = u2[(size_t)jj * np + col];
+      const double c = t.wc[jj];
+      v = double2{v0.x + c * (v1.x - v0.x), v0.y + c * (v1.y - v0.y)};
+    }
+    if (fin) {
+      const double2 w0 = u3[(size_t)jj * np + col], w1 = u3[(size_t)(jj + 1) * np + col];
+      const double c = t.wf[jj];
+      w = double2{w0.x + c * (w1.x - w0.x), w0.y + c * (w1.y - w0.y)};
+    }
+    vcl[col] = v;
+    wfl[col] = w;
+  }
+  __syncthreads();
+  const double2* U = u1 + (size_t)jj * np;
+  const double2* W = u3 + (size_t)jj * np;
+  const double2* V = u2 + (size_t)jj * np;
+  const double2* P = p + (size_t)jj * np;
+  for (int col = threadIdx.x; col < d.np; col += blockDim.x) {
+    const int i = col % d.nkx, kk = col / d.nkx;
+    if (jj < d.nyu) {
+      s[1] += pair_term(U, U, col, i, kk, d.nz, d.nkx);
+      s[5] += pair_term(W, W, col, i, kk, d.nz, d.nkx);
+      s[8] += pair_term(U, vcl, col, i, kk, d.nz, d.nkx);
+      s[9] += pair_term(U, W, col, i, kk, d.nz, d.nkx);
+    }
+    if (jj < d.nyv) {
+      s[3] += pair_term(V, V, col, i, kk, d.nz, d.nkx);
+      s[10] += pair_term(V, wfl, col, i, kk, d.nz, d.nkx);
+    }
+    if (jj < d.nyp) s[7] += pair_term(P, P, col, i, kk, d.nz, d.nkx);
+  }
+  if (threadIdx.x == 0) {
+    if (jj < d.nyu) { s[0] = U[0].x; s[4] = W[0].x; }
+    if (jj < d.nyv) s[2] = V[0].x;
+    if (jj < d.nyp) s[6] = P[0].x;
+  }
+  __shared__ double red[8][11];
+#pragma unroll
+  for (int r = 0; r < 11; ++r) {
+    double x = s[r];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][r] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 11) {
+    double x = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) x += red[w][threadIdx.x];
+    const double scale = (double)d.ngx * (double)d.ngz;
+    acc[(size_t)threadIdx.x * L + jj] += scale * x;
+  }
+}
+
+void launch_stats(const double2* u1, const double2* u2, const double2* u3, const double2* p, double2* vc,
+                  double2* wf, double* acc, const Dims& d, const Tables& t, cudaStream_t st) {
+  const int L = d.nyu > d.nyv ? d.nyu : d.nyv;
+  k_stats<<<L, 256, 0, st>>>(u1, u2, u3, p, vc, wf, acc, d, t, L);
+}
+
+// v interpolated to every centre and w to every face in spectral space (zero
+// on ghost centres and wall faces): the y interpolation the statistics pair
+// u with v and v with w through.
+__global__ void k_stage_itp(const double2* u2, const double2* u3, double2* vc, double2* wf, Dims d, Tables t) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= d.np) return;
+  const int jj = blockIdx.y;
+  const size_t np = d.np, c0 = (size_t)jj * np + col;
+  if (jj < d.nyu) {
+    double2 v = double2{0.0, 0.0};
+    if (jj >= 1 && jj <= d.nyu - 2) {
+      const double2 v0 = u2[c0 - np], v1 = u2[c0];
+      const double c = t.wc[jj];
+      v = double2{v0.x + c * (v1.x - v0.x), v0.y + c * (v1.y - v0.y)};
+    }
+    vc[c0] = v;
+  }
+  if (jj < d.nyv) {
+    double2 w = double2{0.0, 0.0};
+    if (jj >= 1 && jj <= d.nyv - 2) {
+      const double2 w0 = u3[c0], w1 = u3[c0 + np];
+      const double c = t.wf[jj];
+      w = double2{w0.x + c * (w1.x - w0.x), w0.y + c * (w1.y - w0.y)};
+    }
+    wf[c0] = w;
+  }
+}
+
+void launch_stage_itp(const double2* u2, const double2* u3, double2* vc, double2* wf, const Dims& d, const Tables& t,
+                      cudaStream_t st) {
+  dim3 grid((d.np + 255) / 256, d.nyu);
+  k_stage_itp<<<grid, 256, 0, st>>>(u2, u3, vc, wf, d, t);
+}
+
+// Conditional statistics (conddown1/2, condup1/2: stats.f90:110-253; both
+// walls summed as recvXC does, stats.f90:473-512).  One CTA per (grid g,
+// plane j1 of this chunk, in-tile z index kin): for each of the ntilez rows
+// of that z phase and each wall it x-inverts the mixed rows and adds the row
+// folded onto the dnx in-tile x points.  Plane 2*jl + side of the mixed
+// buffers holds wall `side` (0 bottom, 1 top mirrored) of plane j1 = j0 + jl.
+__global__ void __launch_bounds__(128) k_xcond(CondArgs a, Dims d, FftPlan ph, const double2* __restrict__ rtw) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int ngx = d.ngx, h = ngx / 2, hp = h + 1;
+  double2* F = reinterpret_cast<double2*>(smraw);
+  double* rows = reinterpret_cast<double*>(F + 3 * hp);
+  double* acc = rows + 3 * ngx;  // [6][dnx]
+  const int g = blockIdx.z, jl = blockIdx.x, kin = blockIdx.y;
+  const int nj = a.nj[g];
+  if (jl >= nj) return;
+  const int nf = g == 0 ? 3 : (g == 1 ? 2 : 1);
+  const int nq = g == 0 ? 6 : (g == 1 ? 3 : 2);
+  for (int e = threadIdx.x; e < 6 * a.dnx; e += blockDim.x) acc[e] = 0.0;
+  __syncthreads();
+  for (int iz = 0; iz < a.ntz; ++iz) {
+    const size_t rowoff = (size_t)(kin + a.dnz * iz) * d.nkx;
+    for (int side = 0; side < 2; ++side) {
+      const size_t plane = (size_t)(2 * jl + side) * d.mp;
+      const double2* src[3];
+      double* outs[3] = {rows, rows + ngx, rows + 2 * ngx};
+      for (int f = 0; f < nf; ++f) src[f] = a.mix[g][f] + plane + rowoff;
+      x_inverse<double>(src, nf, F, hp, outs, d, ph, rtw);
+      const double sg = side ? -1.0 : 1.0;
+      for (int i = threadIdx.x; i < a.dnx; i += blockDim.x) {
+        double q[6] = {0, 0, 0, 0, 0, 0};
+        for (int ix = 0; ix < a.ntx; ++ix) {
+          const int x = i + a.dnx * ix;
+          const double A = rows[x];
+          if (g == 0) {
+            const double B = rows[ngx + x], C = rows[2 * ngx + x];
+            q[0] += A; q[1] += A * A; q[2] += B; q[3] += B * B; q[4] += A * (sg * C); q[5] += A * B;
+          } else if (g == 1) {
+            const double B = rows[ngx + x];
+            q[0] += sg * A; q[1] += A * A; q[2] += (sg * A) * B;
+          } else {
+            q[0] += A; q[1] += A * A;
+          }
+        }
+        for (int r = 0; r < nq; ++r) acc[r * a.dnx + i] += q[r];
+      }
+      __syncthreads();
+    }
+  }
+  const size_t pl = (size_t)a.dnx * a.dnz;
+  for (int i = threadIdx.x; i < a.dnx; i += blockDim.x)
+    for (int r = 0; r < nq; ++r) {
+      double* o = a.out[g] + (size_t)r * a.njtot[g] * pl + (size_t)(a.j0 + jl) * pl + (size_t)kin * a.dnx + i;
+      *o += acc[r * a.dnx + i];
+    }
+}
+
+void launch_xcond(const CondArgs& a, const Dims& d, const FftPlan& ph, const double2* rtw, cudaStream_t st) {
+  const int njmax = a.nj[0] > a.nj[1] ? (a.nj[0] > a.nj[2] ? a.nj[0] : a.nj[2]) : (a.nj[1] > a.nj[2] ? a.nj[1] : a.nj[2]);
+  if (njmax <= 0) return;
+  dim3 grid(njmax, a.dnz, 3);
+  const int hp = d.ngx / 2 + 1;
+  size_t sm = sizeof(double2) * 3 * (size_t)hp + sizeof(double) * (3 * (size_t)d.ngx + 6 * (size_t)a.dnx);
+  k_xcond<<<grid, 128, sm, st>>>(a, d, ph, rtw);
+}
+
 void launch_spectra(const double2* u1, const double2* u2, const double2* u3, const double2* p, double* sp,
                     const Dims& d, const Tables& t, cudaStream_t st) {
   dim3 grid((d.np + 255) / 256, d.nyu);
@@ -774,7 +922,7 @@ cudaError_t configure_kernels() {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  const cudaError_t r[8] = {allow_smem(k_zinv<double>, optin), allow_smem(k_zinv<float>, optin),
+  const cudaError_t r[9] = {allow_smem(k_xcond, optin), allow_smem(k_zinv<double>, optin), allow_smem(k_zinv<float>, optin),
                             allow_smem(k_zfwd<double>, optin), allow_smem(k_zfwd<float>, optin),
                             allow_smem(k_xprod<double>, optin), allow_smem(k_xprod<float>, optin),
                             allow_smem(k_xmask<double>, optin), allow_smem(k_xmask<float>, optin)};

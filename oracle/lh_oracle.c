@@ -378,6 +378,8 @@ struct lho {
   /* statistics */
   int istat;
   double* stat;   /* 13 profiles */
+  int icond, nju, njv, njp, dnx, dnz;
+  double* cond;   /* conditional statistics, see lho_cond_get */
   int nspec;
   double *spU, *spV, *spW, *spUV, *spP;
   int nthreads;
@@ -631,7 +633,7 @@ void lho_destroy(lho* s) {
   free(s->ibu_j); free(s->ibv_j); free(s->ibu_mask); free(s->ibv_mask);
   double* f[] = {s->u1, s->u2, s->u3, s->p, s->nu1, s->nu2, s->nu3, s->r1, s->r2, s->r3, s->ly1, s->ly2,
                  s->ly3, s->psi, s->div, s->pUU, s->pUW, s->pWW, s->pVV, s->pUV, s->pVW, s->dg1, s->dg2,
-                 s->dg3, s->stat, s->spU, s->spV, s->spW, s->spUV, s->spP};
+                 s->dg3, s->stat, s->spU, s->spV, s->spW, s->spUV, s->spP, s->cond};
   for (size_t i = 0; i < sizeof f / sizeof f[0]; ++i) free(f[i]);
   fft_plan_free(&s->zplan);
   rfft_plan_free(&s->xplan);
@@ -736,6 +738,15 @@ lho* lho_create(const lho_config* cfg, char* err, int errlen) {
   s->spW = (double*)xcalloc((size_t)s->nyu * s->nplane, 8);
   s->spUV = (double*)xcalloc((size_t)s->nyu * s->nplane, 8);
   s->spP = (double*)xcalloc((size_t)s->nyp * s->nplane, 8);
+  if (cfg->geometry_type == 3) {
+    s->dnx = s->ngx / cfg->ntilex;
+    s->dnz = s->ngz / cfg->ntilez;
+    s->nju = N[3][1] - N[3][0] + 1;
+    s->njv = N[2][1] - N[2][0] + 1;
+    s->njp = N[3][1] - N[3][0] - 1;
+    const size_t pl = (size_t)s->dnx * s->dnz;
+    s->cond = (double*)xcalloc(pl * (6 * (size_t)s->nju + 3 * (size_t)s->njv + 2 * (size_t)s->njp), 8);
+  }
   return s;
 }
 
@@ -1469,4 +1480,102 @@ int lho_stats_get(const lho* s, double* out) {
   const int L = s->nyu > s->nyv ? s->nyu : s->nyv;
   memcpy(out, s->stat, sizeof(double) * 13 * (size_t)L);
   return s->istat;
+}
+
+/* Conditional statistics (conddown1/2, condup1/2: stats.f90:110-253) of the
+ * wall bands, summed over both walls as recvXC does (stats.f90:473-512): the
+ * bottom band's planes counted from its wall (u: j = N(4,0)+j1, v: N(3,0)+j1,
+ * p: N(4,0)+1+j1) plus the top band's planes counted from the top wall
+ * (u: N(4,3)+1-j1, v: N(3,3)+1-j1, p: N(4,3)-j1) with v's sign flipped.
+ * Each entry sums a field over the ntilex x ntilez tiles at one in-tile point.
+ * Layout of lho_cond_get's output: 11 blocks [j1][kin][i] (i fastest):
+ * UmC U2mC WmC W2mC UVmC UWmC (nju planes), VmC V2mC VWmC (njv), PmC P2mC (njp). */
+void lho_cond_accumulate(lho* s) {
+  if (!s->cond) return;
+  const int nc = s->nplane, ngx = s->ngx, ngz = s->ngz, dnx = s->dnx, dnz = s->dnz;
+  const int tx = s->cfg.ntilex, tz = s->cfg.ntilez;
+  const size_t PL = (size_t)ngx * ngz, pl = (size_t)dnx * dnz;
+  double* vi = (double*)xcalloc(2 * (size_t)s->nyu * nc, 8);
+  double* wi = (double*)xcalloc(2 * (size_t)s->nyv * nc, 8);
+  v_to_centres(s, vi);
+  for (int jj = 1; jj < s->nyv - 1; ++jj) {
+    const int j = jj + s->jv0;
+    const double wf = (YV(s, j) - YU(s, j)) / (YU(s, j + 1) - YU(s, j));
+    const size_t c0 = 2 * (size_t)(j - s->ju0) * nc, c1 = c0 + 2 * (size_t)nc;
+    for (size_t n = 0; n < 2 * (size_t)nc; ++n)
+      wi[2 * (size_t)jj * nc + n] = s->u3[c0 + n] + wf * (s->u3[c1 + n] - s->u3[c0 + n]);
+  }
+  double* blk[11];
+  blk[0] = s->cond;
+  for (int q = 1; q < 11; ++q) {
+    const int nj = q <= 6 ? s->nju : (q <= 9 ? s->njv : s->njp);  /* size of block q-1 */
+    blk[q] = blk[q - 1] + (size_t)nj * pl;
+  }
+  const size_t sl = plane_scratch_len(s);
+  double* scr = (double*)xcalloc(sl, 8);
+  double* A = (double*)xcalloc(PL, 8);
+  double* B = (double*)xcalloc(PL, 8);
+  double* C = (double*)xcalloc(PL, 8);
+  for (int side = 0; side < 2; ++side) {
+    const double sg = side ? -1.0 : 1.0;
+    for (int j1 = 0; j1 < s->nju; ++j1) {
+      const int ju = side ? s->nyu - 1 - j1 : j1;
+      plane_to_phys_(s, s->u1 + 2 * (size_t)ju * nc, A, scr);
+      plane_to_phys_(s, s->u3 + 2 * (size_t)ju * nc, B, scr);
+      plane_to_phys_(s, vi + 2 * (size_t)ju * nc, C, scr);
+      for (int k = 0; k < dnz; ++k)
+        for (int i = 0; i < dnx; ++i) {
+          double a[6] = {0, 0, 0, 0, 0, 0};
+          for (int iz = 0; iz < tz; ++iz)
+            for (int ix = 0; ix < tx; ++ix) {
+              const size_t n = (size_t)(k + dnz * iz) * ngx + i + dnx * ix;
+              a[0] += A[n]; a[1] += A[n] * A[n]; a[2] += B[n]; a[3] += B[n] * B[n];
+              a[4] += A[n] * (sg * C[n]); a[5] += A[n] * B[n];
+            }
+          for (int q = 0; q < 6; ++q) blk[q][(size_t)j1 * pl + (size_t)k * dnx + i] += a[q];
+        }
+    }
+    for (int j1 = 0; j1 < s->njv; ++j1) {
+      const int jv = side ? s->nyv - 1 - j1 : j1;
+      plane_to_phys_(s, s->u2 + 2 * (size_t)jv * nc, A, scr);
+      plane_to_phys_(s, wi + 2 * (size_t)jv * nc, B, scr);
+      for (int k = 0; k < dnz; ++k)
+        for (int i = 0; i < dnx; ++i) {
+          double a[3] = {0, 0, 0};
+          for (int iz = 0; iz < tz; ++iz)
+            for (int ix = 0; ix < tx; ++ix) {
+              const size_t n = (size_t)(k + dnz * iz) * ngx + i + dnx * ix;
+              a[0] += sg * A[n]; a[1] += A[n] * A[n]; a[2] += (sg * A[n]) * B[n];
+            }
+          for (int q = 0; q < 3; ++q) blk[6 + q][(size_t)j1 * pl + (size_t)k * dnx + i] += a[q];
+        }
+    }
+    for (int j1 = 0; j1 < s->njp; ++j1) {
+      const int jp = side ? s->nyp - 1 - j1 : j1;
+      plane_to_phys_(s, s->p + 2 * (size_t)jp * nc, A, scr);
+      for (int k = 0; k < dnz; ++k)
+        for (int i = 0; i < dnx; ++i) {
+          double a[2] = {0, 0};
+          for (int iz = 0; iz < tz; ++iz)
+            for (int ix = 0; ix < tx; ++ix) {
+              const size_t n = (size_t)(k + dnz * iz) * ngx + i + dnx * ix;
+              a[0] += A[n]; a[1] += A[n] * A[n];
+            }
+          for (int q = 0; q < 2; ++q) blk[9 + q][(size_t)j1 * pl + (size_t)k * dnx + i] += a[q];
+        }
+    }
+  }
+  free(scr); free(A); free(B); free(C); free(vi); free(wi);
+  s->icond++;
+}
+
+/* out: the 11 blocks described above; returns the number of accumulations.
+ * dims[0..4] = nju, njv, njp, dnx, dnz (all 0 without canopies). */
+int lho_cond_get(const lho* s, double* out, int32_t* dims) {
+  if (dims) { dims[0] = s->nju; dims[1] = s->njv; dims[2] = s->njp; dims[3] = s->dnx; dims[4] = s->dnz; }
+  if (out && s->cond) {
+    const size_t pl = (size_t)s->dnx * s->dnz;
+    memcpy(out, s->cond, 8 * pl * (6 * (size_t)s->nju + 3 * (size_t)s->njv + 2 * (size_t)s->njp));
+  }
+  return s->icond;
 }

@@ -152,6 +152,10 @@ void lho_stats_accumulate(lho* s);
 /* out: 13 profiles, each of length nyu (U,U2,W,W2,UV,UW,P(on u index range),P2) or nyv (V,V2,VW,wx,wx2)
  * packed as described in lh_oracle.c::lho_stats_get. Returns istat. */
 int  lho_stats_get(const lho* s, double* out);
+/* Conditional statistics of the wall bands (conddown/condup, stats.f90:110-253),
+ * both walls summed as write_stats does; see lh_oracle.c for the layout. */
+void lho_cond_accumulate(lho* s);
+int  lho_cond_get(const lho* s, double* out, int32_t* dims);
 void lho_spectra_accumulate(lho* s);
 void lho_spectra_get(const lho* s, double* spU, double* spV, double* spW, double* spUV, double* spP);
 

@@ -96,6 +96,8 @@ def lib():
         L.lho_stats_accumulate.argtypes = [C.c_void_p]
         L.lho_stats_get.argtypes = [C.c_void_p, _dp]
         L.lho_spectra_accumulate.argtypes = [C.c_void_p]
+        L.lho_cond_accumulate.argtypes = [C.c_void_p]
+        L.lho_cond_get.argtypes = [C.c_void_p, _dp, C.c_void_p]
         L.lho_spectra_get.argtypes = [C.c_void_p] + [_dp] * 5
         L.lho_fft_c2c.argtypes = [C.c_int, C.c_int, _dp]
         L.lho_rft.argtypes = [C.c_int, C.c_int, _dp]
@@ -270,6 +272,25 @@ class Oracle:
 
     def spectra_accumulate(self):
         lib().lho_spectra_accumulate(self.h)
+
+    COND_ROWS = ("UmC", "U2mC", "WmC", "W2mC", "UVmC", "UWmC", "VmC", "V2mC", "VWmC", "PmC", "P2mC")
+
+    def cond_accumulate(self):
+        lib().lho_cond_accumulate(self.h)
+
+    def cond(self):
+        """(count, dict name -> array [j1][kin][i]) of the conditional statistics."""
+        dims = np.zeros(5, np.int32)
+        lib().lho_cond_get(self.h, None, dims.ctypes.data)
+        nju, njv, njp, dnx, dnz = [int(x) for x in dims]
+        sizes = [nju] * 6 + [njv] * 3 + [njp] * 2
+        out = np.zeros(sum(sizes) * dnx * dnz)
+        n = lib().lho_cond_get(self.h, _p(out) if out.size else None, dims.ctypes.data)
+        res, off = {}, 0
+        for name, nj in zip(self.COND_ROWS, sizes):
+            res[name] = out[off:off + nj * dnx * dnz].reshape(nj, dnz, dnx)
+            off += nj * dnx * dnz
+        return n, res
 
     def spectra(self):
         nc = self.nz * self.nkx

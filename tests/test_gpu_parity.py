@@ -122,3 +122,38 @@ def test_step_is_graph_replay(oracle_mod):
     s.step(3)
     ms, launches = s.last_step_ms()
     assert ms > 0 and launches > 0
+
+
+def test_plane_statistics(oracle_mod):
+    o, s = _pair(oracle_mod, SMALL)
+    o.step(2)
+    s.step(2)
+    for _ in range(2):
+        o.stats_accumulate()
+        s.stats_accumulate()
+    n, st = s.stats_flush()
+    no, so = o.stats()
+    assert n == no == 2
+    ny = {"u": s.nyu, "v": s.nyv, "p": s.nyp}
+    for r, (name, grid) in enumerate(zip(s.STAT_ROWS, "uuvvuuppuuv")):
+        a, b = st[name], so[r, :ny[grid]]
+        # means of v vanish by continuity: an absolute floor of 1e-13 per summed point covers round-off
+        tol = 1e-11 * np.abs(b).max() + 1e-13 * s.ngx * s.ngz
+        assert np.abs(a - b).max() < tol, f"{name}: {np.abs(a - b).max():.3e} >= {tol:.3e}"
+
+
+def test_conditional_statistics(oracle_mod):
+    o, s = _pair(oracle_mod, SMALL)
+    o.step(1)
+    s.step(1)
+    for _ in range(2):
+        o.cond_accumulate()
+        s.cond_accumulate()
+    n, cg = s.cond_flush()
+    no, co = o.cond()
+    assert n == no == 2
+    for name in s.COND_ROWS:
+        a, b = cg[name], co[name]
+        assert a.shape == b.shape, name
+        tol = 1e-11 * np.abs(b).max() + 1e-13 * s.ngx * s.ngz
+        assert np.abs(a - b).max() < tol, f"{name}: {np.abs(a - b).max():.3e} >= {tol:.3e}"

@@ -106,3 +106,31 @@ def test_tridiagonal_matches_dense(oracle_mod):
     rhs = rng.standard_normal(n)
     x = oracle_mod.tridiag_solve(a1, a2, a3, rhs)
     assert np.abs(x - np.linalg.solve(A, rhs)).max() < 1e-13
+
+
+def _parseval_sum(f, g, ngx, ngz):
+    """sum over the padded physical plane of f*g from the spectral planes f, g
+    (nz x nkx), with the real x-inverse's treatment of the kx = 0 line."""
+    nz, nkx = f.shape
+    tot = 2.0 * np.sum((f[:, 1:] * np.conj(g[:, 1:])).real)
+    kk = np.arange(nz)
+    pk = (nz - kk) % nz
+    re = (f[:, 0] * np.conj(g[:, 0])).real
+    cross = (f[:, 0] * g[pk, 0]).real
+    line = 0.5 * (re + cross)
+    line[nz // 2] = 0.5 * re[nz // 2]
+    return ngx * ngz * (tot + line.sum())
+
+
+def test_plane_sums_by_parseval(oracle_mod):
+    """The identity the GPU statistics rely on: physical-plane sums of products
+    equal weighted sums over the spectral coefficients, also for a kx = 0 line
+    that is not Hermitian (its imaginary part is dropped by the inverse)."""
+    o = oracle_mod.Oracle(**SMALL)
+    rng = np.random.default_rng(5)
+    f = rng.standard_normal((o.nz, o.nkx)) + 1j * rng.standard_normal((o.nz, o.nkx))
+    g = rng.standard_normal((o.nz, o.nkx)) + 1j * rng.standard_normal((o.nz, o.nkx))
+    pf, pg = o.to_phys(f), o.to_phys(g)
+    assert abs((pf * pg).sum() - _parseval_sum(f, g, o.ngx, o.ngz)) < 1e-12 * abs((pf * pg).sum()) + 1e-10
+    assert abs((pf * pf).sum() - _parseval_sum(f, f, o.ngx, o.ngz)) < 1e-12 * (pf * pf).sum()
+    assert abs(pf.sum() - o.ngx * o.ngz * f[0, 0].real) < 1e-10
