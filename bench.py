@@ -117,6 +117,7 @@ class ClockSampler:
 # model counts for the roofline
 # ----------------------------------------------------------------------------
 def _stages(n: int):
+    """Radices of the DIT passes, in the order the kernels run them: 4s, 2s, 3s."""
     m, n4, n2, n3 = n, 0, 0, 0
     while m % 4 == 0:
         m //= 4
@@ -127,39 +128,61 @@ def _stages(n: int):
     while m % 3 == 0:
         m //= 3
         n3 += 1
-    return [3] * n3 + [2] * n2 + [4] * n4
+    return [4] * n4 + [2] * n2 + [3] * n3
 
 
-def fft_flops(n: int) -> float:
-    """Real FP64 operations (FMA = 2) of one complex DIF of length n as the kernels
-    execute it: per butterfly r=4: 16 + 18 twiddle, r=2: 4 + 6, r=3: 16 + 12; the
-    last stage has no twiddles."""
+def fft_flops(n: int, prune_last: bool = False) -> float:
+    """FP64 operations (FMA = 2) of one complex DIT of length n as the kernels
+    execute it.  Per butterfly with twiddles fused into the additions:
+    radix 4: 38 (16 without twiddles), radix 2: 12 (4), radix 3: 32 (18), and
+    28 for a last radix-3 stage whose middle output is skipped.  The first
+    stage has no twiddles."""
     rad = _stages(n)
     tot = 0.0
     for s, r in enumerate(rad):
-        last = s == len(rad) - 1
-        base = {4: 16, 2: 4, 3: 16}[r]
-        tw = 0 if last else {4: 18, 2: 6, 3: 12}[r]
-        tot += (n / r) * (base + tw)
+        first, last = s == 0, s == len(rad) - 1
+        if first:
+            per = {4: 16, 2: 4, 3: 18}[r]
+        else:
+            per = {4: 38, 2: 12, 3: 32}[r]
+            if last and prune_last and r == 3:
+                per = 28
+        tot += (n / r) * per
     return tot
 
 
 def xprod_flops(ngx, ngz, nkx, nlev) -> float:
-    """x-pass with products for one substage: per level and z row, 3 inverse
-    and 6 forward real transforms (complex DIF of ngx/2 plus pre/post
-    processing), interpolation and products."""
+    """x-pass with products for one substage, per level and z row: u and w
+    inverted together by one complex transform of length ngx, v by a half-length
+    real transform (pre-processing 12 per mode), six products forwarded as three
+    pairs (split 8 per kept mode), interpolation and products 15 per point."""
     h = ngx // 2
-    inv = fft_flops(h) + 12.0 * h
-    fwd = fft_flops(h) + 18.0 * nkx
-    prod = ngx * (6 + 3 * 3)
-    return nlev * ngz * (3 * inv + 6 * fwd + prod)
+    inv = fft_flops(ngx) + 8.0 * nkx + fft_flops(h) + 12.0 * h
+    fwd = 3 * (fft_flops(ngx) + 16.0 * nkx)
+    prod = 15.0 * ngx
+    return nlev * ngz * (inv + fwd + prod)
 
 
-def z_flops(ngz, nkx, nplanes) -> float:
-    return nplanes * nkx * fft_flops(ngz)
+def z_flops(ngz, nkx, nplanes, prune_last=False) -> float:
+    return nplanes * nkx * fft_flops(ngz, prune_last)
 
 
 # ----------------------------------------------------------------------------
+def max_over_ranks(value: float, dist, device: str) -> float:
+    """The slowest rank's timing (replicas only: no data moves between ranks)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(world: int, points_per_rank: int, steps: int, ms_max: float) -> float:
+    """Grid-point RK3 steps per second of all replicas together."""
+    return world * points_per_rank * steps / (ms_max / 1e3)
+
+
 def build_solver(cfg: dict, precision: int, seed: int):
     import littleharsh_gb300 as lh
     from littleharsh_gb300.initial import initial_field
@@ -218,6 +241,57 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+def ensemble_configs():
+    """Configuration 4: 16 replicas of uneven sizes, canopy pitches pi/6, pi/8,
+    pi/12 (12x6, 16x8, 24x12 tiles), heights 0.1/0.2, Re_b 2800-6900
+    (Re_tau ~180-395), posts a quarter of the pitch wide."""
+    sizes = [(144, 129, 12)] * 6 + [(192, 193, 16)] * 6 + [(288, 257, 24)] * 4
+    tiles = [(12, 6), (16, 8), (24, 12)]
+    res = [2800.0, 4500.0, 6900.0]
+    out = []
+    for i, (ng, ny, dsty) in enumerate(sizes):
+        tx, tz = tiles[i % 3]
+        out.append(dict(Re=res[i % 3], alp=1.0, bet=2.0, ngalx=ng, ngalz=ng, ny=ny, dyq=13.6, ppp=5, geometry_type=3,
+                        posth=(0.1, 0.2)[i % 2], dsty=dsty, dstx=max(1, ng // tx // 4), dstz=max(1, ng // tz // 4),
+                        ntilex=tx, ntilez=tz, flag_ctpress=0))
+    return out
+
+
+def run_ensemble(args, rank: int, world: int):
+    import littleharsh_gb300 as lh
+    cfgs = ensemble_configs()
+    prec = lh.PREC_MIXED if args.precision == "mixed" else lh.PREC_FP64
+    members = [build_solver(c, prec, seed=100 + i)[0] for i, c in enumerate(cfgs)]
+    pts = sum(m.ngx * m.ngz * m.nyu for m in members)
+    e = lh.Ensemble(members)
+    e.step(max(args.warmup, 1))
+    sampler = ClockSampler(0)
+    sampler.start()
+    ms = e.step(args.steps)
+    clocks = sampler.stop()
+    # the same replicas one by one, each with its own graph
+    for m in members:
+        m.step(1)
+    seq = 0.0
+    for m in members:
+        m.step(args.steps)
+        seq += m.last_step_ms()[0]
+    value = pts * args.steps / (ms / 1e3)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == lh.PREC_FP64 else "mixed f32/f64",
+            "data": "synthetic (seeded laminar + 10% perturbation, projected divergence-free)",
+            "config": {"workload": "ensemble16_config4", "replicas": len(members),
+                       "grids": sorted({(m.ngx, m.ngz, m.nyu) for m in members}), "precision": args.precision},
+            "sequential": {"value": pts * args.steps / (seq / 1e3), "ms_per_step": seq / args.steps},
+            "speedup_vs_sequential": seq / ms, "gpu_launches": sum(m.last_step_ms()[1] for m in members) * args.steps,
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+    e.close()
+    for m in members:
+        m.close()
+
+
 def run_ours(args, rank: int, world: int, local_rank: int, dist):
     import littleharsh_gb300 as lh
     cfg = WORKLOADS[args.workload]
@@ -244,13 +318,8 @@ def run_ours(args, rank: int, world: int, local_rank: int, dist):
     barrier()
     clocks = sampler.stop()
     ms, launches = s.last_step_ms()
-    ms_max = ms
-    if dist is not None:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{local_rank}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = world * pts * args.steps / (ms_max / 1e3)
+    ms_max = max_over_ranks(ms, dist, f"cuda:{local_rank}")
+    value = whole_job_value(world, pts, args.steps, ms_max)
     out = None
     if rank == 0:
         peaks = _peaks()
@@ -266,7 +335,8 @@ def run_ours(args, rank: int, world: int, local_rank: int, dist):
         model = {
             "zinv": ((2 * nl_u + nl_v) * (npl * 16 + mp * csz), z_flops(s.ngz, s.nkx, 2 * nl_u + nl_v)),
             "xprod": ((2 * nl_u + nl_v + 4 * nl_u + 2 * nl_v) * mp * csz, xprod_flops(s.ngx, s.ngz, s.nkx, nl_u)),
-            "zfwd": ((4 * nl_u + 2 * nl_v) * (mp * csz + npl * 16), z_flops(s.ngz, s.nkx, 4 * nl_u + 2 * nl_v)),
+            "zfwd": ((4 * nl_u + 2 * nl_v) * (mp * csz + npl * 16),
+                     z_flops(s.ngz, s.nkx, 4 * nl_u + 2 * nl_v, prune_last=(s.ngz % 3 == 0 and s.nz * 3 == 2 * s.ngz))),
             "assemble": (19 * s.nyu * npl * 16, 0.0),
             "vsolve": (4 * (2 * s.nyu + s.nyv) * npl * 16, 0.0),
             "psolve": ((16 + 16 + 16 + 8 + 8) * s.nyp * npl + 14 * 16 * s.nyp * npl, 0.0),
@@ -336,6 +406,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ensemble", action="store_true", help="configuration 4: 16 replicas in one graph per step")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -355,7 +426,10 @@ def main():
             torch.cuda.set_device(0)
         except Exception:
             pass
-    run_ours(args, rank, world, local_rank, dist)
+    if args.ensemble:
+        run_ensemble(args, rank, world)
+    else:
+        run_ours(args, rank, world, local_rank, dist)
     if dist is not None:
         dist.destroy_process_group()
 

@@ -64,6 +64,7 @@ enum { LH_LAYOUT_PLANES = 0, LH_LAYOUT_COLUMNS = 1 };
 enum { LH_PREC_FP64 = 0, LH_PREC_MIXED = 1 };
 
 typedef struct lh_handle lh_handle;
+typedef struct lh_ensemble lh_ensemble;
 
 /* Everything lh_init needs besides the grid arrays.  Integer arrays follow
  * the reference's Fortran storage: N(1:4,0:nband+1) is N[(band)*4 + row-1]. */
@@ -171,6 +172,17 @@ int lh_stats_flush(lh_handle* h, double* out, int32_t* count, int32_t reset);
  * V2mC VWmC (njv), PmC P2mC (njp).  Call between steps. */
 int lh_cond_accumulate(lh_handle* h);
 int lh_cond_flush(lh_handle* h, double* out, int32_t* dims5, int32_t* count, int32_t reset);
+
+/* Ensembles of independent replicas (uneven grids and geometries allowed) on
+ * one device: lh_ensemble_step advances every member by nsteps RK3 steps with
+ * one CUDA-graph launch per step; the graph forks into each member's stream,
+ * so the members' kernels run concurrently.  Members keep their own state and
+ * can still be used alone.  ms (may be NULL) receives the device time.  No
+ * counterpart in the reference (one simulation per MPI job). */
+int lh_ensemble_create(lh_handle* const* members, int32_t n, lh_ensemble** out);
+int lh_ensemble_step(lh_ensemble* e, int32_t nsteps, double* ms);
+const char* lh_ensemble_last_error(const lh_ensemble* e);
+void lh_ensemble_free(lh_ensemble* e);
 
 /* Device time of the last lh_rk3_step call in milliseconds (CUDA events on
  * the handle's stream) and the number of kernels one step launches. */

@@ -31,7 +31,8 @@ EXPORTED_SYMBOLS = [
     "lh_get_nonlinear", "lh_set_time", "lh_get_time", "lh_rk3_step", "lh_substage", "lh_get_rhs", "lh_divmax",
     "lh_cfl_dt", "lh_project", "lh_spectra_accumulate", "lh_spectra_flush", "lh_stats_accumulate",
     "lh_stats_flush", "lh_cond_accumulate", "lh_cond_flush", "lh_last_step_ms", "lh_profile_step",
-    "lh_project_noalloc", "lh_write_restart", "lh_read_restart", "lh_write_stats", "lh_write_spectra", "lh_read_input", "lh_setup_grid", "lh_setup_canopy",
+    "lh_project_noalloc", "lh_ensemble_create", "lh_ensemble_step", "lh_ensemble_last_error",
+    "lh_ensemble_free", "lh_write_restart", "lh_read_restart", "lh_write_stats", "lh_write_spectra", "lh_read_input", "lh_setup_grid", "lh_setup_canopy",
 ]
 
 
@@ -118,6 +119,12 @@ def load_library(build: bool = True) -> C.CDLL:
     L.lh_read_restart.argtypes = [vp, cp, cp, _dp, C.POINTER(i32)]
     L.lh_write_stats.argtypes = [vp, C.POINTER(Params)] + [_dp] * 4 + [cp, i32]
     L.lh_write_spectra.argtypes = [vp, C.POINTER(Params)] + [_dp] * 4 + [cp, cp, i32]
+    L.lh_ensemble_create.argtypes = [C.c_void_p, i32, C.POINTER(vp)]
+    L.lh_ensemble_step.argtypes = [vp, i32, _dp]
+    L.lh_ensemble_last_error.argtypes = [vp]
+    L.lh_ensemble_last_error.restype = cp
+    L.lh_ensemble_free.argtypes = [vp]
+    L.lh_ensemble_free.restype = None
     L.lh_read_input.argtypes = [cp, C.POINTER(Input)]
     L.lh_setup_grid.argtypes = [C.POINTER(Input), C.POINTER(Params)] + [_dp] * 6
     L.lh_setup_canopy.argtypes = [C.POINTER(Input), C.POINTER(Params), C.c_void_p, C.POINTER(i32), C.c_void_p,
@@ -392,6 +399,39 @@ class Solver:
         n = C.c_int32(0)
         self._check(load_library().lh_spectra_flush(self.h, *[_p(x) for x in o], C.byref(n), int(reset)))
         return n.value, o
+
+
+class Ensemble:
+    """Independent solvers advanced together, one CUDA graph launch per RK3 step."""
+
+    def __init__(self, members):
+        self.members = list(members)
+        L = load_library()
+        arr = (C.c_void_p * len(self.members))(*[m.h.value for m in self.members])
+        e = C.c_void_p()
+        rc = L.lh_ensemble_create(arr, len(self.members), C.byref(e))
+        if rc:
+            raise LhError(f"lh_ensemble_create failed ({rc}): {L.lh_last_error(None).decode()}")
+        self.e = e
+
+    def step(self, n: int = 1) -> float:
+        ms = C.c_double(0)
+        L = load_library()
+        rc = L.lh_ensemble_step(self.e, n, C.byref(ms))
+        if rc:
+            raise LhError(f"lh_ensemble_step failed ({rc}): {L.lh_ensemble_last_error(self.e).decode()}")
+        return ms.value
+
+    def close(self):
+        if getattr(self, "e", None):
+            load_library().lh_ensemble_free(self.e)
+            self.e = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 from .initial import initial_field  # noqa: E402

@@ -74,7 +74,7 @@ struct lh_handle {
   int *cond_ul = nullptr, *cond_vl = nullptr, *cond_pl = nullptr;
   double* tabs = nullptr;  // lu_u, lu_v, u11 (rewritten when dt changes)
   DevScalars* sc = nullptr;
-  PlanStore pz, ph;
+  PlanStore pz, ph, pf;  // z (Ngalz), x half length (Ngalx/2), x full length (Ngalx)
   double2* rtw = nullptr;
   int tx = 8, chunk = 16;
   // state
@@ -304,7 +304,7 @@ int enqueue_substage(lh_handle* h, int k, int upto) {
     a.wc = h->t.wc; a.wf = h->t.wf; a.dyc = h->t.dyc;
     a.dxi = d.ngx / h->Lx; a.dzi = d.ngz / h->Lz;
     a.sc = h->sc; a.want_cfl = 0; a.chunk = h->chunk;
-    launch_xprod<R>(a, d, h->ph.plan, h->rtw, st);
+    launch_xprod<R>(a, d, h->ph.plan, h->pf.plan, h->rtw, st);
     mark(h, K_XPROD);
   }
   {
@@ -547,7 +547,9 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
   }
   int rc;
   // FFT plans: z of length ngz, x through a complex transform of ngx/2
-  if ((rc = build_plan(h, h->pz, d.ngz, d.nz / 2)) || (rc = build_plan(h, h->ph, d.ngx / 2, 0))) return bail(rc);
+  if ((rc = build_plan(h, h->pz, d.ngz, d.nz / 2)) || (rc = build_plan(h, h->ph, d.ngx / 2, 0)) ||
+      (rc = build_plan(h, h->pf, d.ngx, 0)))
+    return bail(rc);
   {
     std::vector<double2> rt(d.ngx / 2 + 1);
     for (int k = 0; k <= d.ngx / 2; ++k) {
@@ -874,6 +876,124 @@ int lh_rk3_step(lh_handle* h, int32_t nsteps) {
   return LH_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Ensembles: one CUDA graph per RK3 step for several independent handles.
+// ---------------------------------------------------------------------------
+struct lh_ensemble {
+  std::vector<lh_handle*> hs;
+  int device = 0;
+  cudaStream_t origin = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  std::vector<cudaEvent_t> ev;  // fork event, then one join event per member
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  double last_ms = 0;
+  std::string err;
+};
+
+namespace {
+void ens_release(lh_ensemble* e) {
+  if (e->graph) cudaGraphExecDestroy(e->graph);
+  for (cudaEvent_t x : e->ev) cudaEventDestroy(x);
+  if (e->t0) cudaEventDestroy(e->t0);
+  if (e->t1) cudaEventDestroy(e->t1);
+  if (e->origin) cudaStreamDestroy(e->origin);
+}
+int ens_fail(lh_ensemble* e, int code, const char* msg, cudaError_t ce = cudaSuccess) {
+  e->err = msg;
+  if (ce != cudaSuccess) { e->err += ": "; e->err += cudaGetErrorString(ce); }
+  return code;
+}
+}  // namespace
+
+int lh_ensemble_create(lh_handle* const* hs, int32_t n, lh_ensemble** out) {
+  if (!out) return LH_EINVAL;
+  *out = nullptr;
+  if (!hs || n < 1) return fail(nullptr, LH_EINVAL, "ensemble needs at least one handle");
+  for (int i = 0; i < n; ++i) {
+    if (!hs[i]) return fail(nullptr, LH_EINVAL, "NULL handle in the ensemble");
+    if (hs[i]->device != hs[0]->device) return fail(nullptr, LH_EINVAL, "ensemble members must share one device");
+    for (int j = 0; j < i; ++j)
+      if (hs[j] == hs[i] || hs[j]->st == hs[i]->st) return fail(nullptr, LH_EINVAL, "ensemble members need distinct streams");
+  }
+  lh_ensemble* e = new lh_ensemble();
+  e->hs.assign(hs, hs + n);
+  e->device = hs[0]->device;
+  cudaSetDevice(e->device);
+  cudaError_t ce = cudaStreamCreateWithFlags(&e->origin, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e->t0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e->t1);
+  for (int i = 0; i <= n && ce == cudaSuccess; ++i) {
+    cudaEvent_t x;
+    ce = cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
+    if (ce == cudaSuccess) e->ev.push_back(x);
+  }
+  if (ce != cudaSuccess) {
+    ens_release(e);
+    delete e;
+    return fail(nullptr, LH_ECUDA, "ensemble set-up: %s", cudaGetErrorString(ce));
+  }
+  *out = e;
+  return LH_OK;
+}
+
+void lh_ensemble_free(lh_ensemble* e) {
+  if (!e) return;
+  cudaSetDevice(e->device);
+  if (e->origin) cudaStreamSynchronize(e->origin);
+  ens_release(e);
+  delete e;
+}
+
+const char* lh_ensemble_last_error(const lh_ensemble* e) { return e ? e->err.c_str() : ""; }
+
+int lh_ensemble_step(lh_ensemble* e, int32_t nsteps, double* ms) {
+  if (!e) return LH_EINVAL;
+  if (nsteps < 0) return ens_fail(e, LH_EINVAL, "nsteps < 0");
+  for (lh_handle* h : e->hs)
+    if (!h->have_fields || !h->have_dt) return ens_fail(e, LH_ESTATE, "every member needs fields and dt");
+  cudaSetDevice(e->device);
+  if (!e->graph) {
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamBeginCapture(e->origin, cudaStreamCaptureModeThreadLocal);
+    if (ce != cudaSuccess) return ens_fail(e, LH_ECUDA, "capture", ce);
+    int rc = LH_OK;
+    cudaEventRecord(e->ev[0], e->origin);
+    for (size_t i = 0; i < e->hs.size() && rc == LH_OK; ++i) {
+      lh_handle* h = e->hs[i];
+      cudaStreamWaitEvent(h->st, e->ev[0], 0);
+      for (int k = 0; k < 3 && rc == LH_OK; ++k) rc = substage(h, k, 5);
+      cudaEventRecord(e->ev[i + 1], h->st);
+      cudaStreamWaitEvent(e->origin, e->ev[i + 1], 0);
+    }
+    ce = cudaStreamEndCapture(e->origin, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return ens_fail(e, rc, "capture of a member failed");
+    }
+    if (ce != cudaSuccess) return ens_fail(e, LH_ECUDA, "capture", ce);
+    ce = cudaGraphInstantiate(&e->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) { e->graph = nullptr; return ens_fail(e, LH_ECUDA, "instantiate", ce); }
+  }
+  cudaEventRecord(e->t0, e->origin);
+  for (int n = 0; n < nsteps; ++n) {
+    cudaError_t ce = cudaGraphLaunch(e->graph, e->origin);
+    if (ce != cudaSuccess) return ens_fail(e, LH_ECUDA, "graph launch", ce);
+  }
+  cudaEventRecord(e->t1, e->origin);
+  cudaError_t ce = cudaEventSynchronize(e->t1);
+  if (ce != cudaSuccess) return ens_fail(e, LH_ECUDA, "ensemble step", ce);
+  float t = 0.f;
+  cudaEventElapsedTime(&t, e->t0, e->t1);
+  e->last_ms = t;
+  if (ms) *ms = t;
+  for (lh_handle* h : e->hs) {
+    h->t_now += nsteps * h->dt;
+    h->iter += nsteps;
+  }
+  return LH_OK;
+}
+
 int lh_last_step_ms(lh_handle* h, double* ms, int32_t* launches) {
   if (!h) return LH_EINVAL;
   if (ms) *ms = h->last_ms;
@@ -951,7 +1071,7 @@ int lh_cfl_dt(lh_handle* h, double cfl, double* dt_out) {
     a.wc = h->t.wc; a.wf = h->t.wf; a.dyc = h->t.dyc;
     a.dxi = d.ngx / h->Lx; a.dzi = d.ngz / h->Lz;
     a.sc = h->sc; a.want_cfl = 1; a.chunk = h->chunk;
-    launch_xprod<R>(a, d, h->ph.plan, h->rtw, h->st);
+    launch_xprod<R>(a, d, h->ph.plan, h->pf.plan, h->rtw, h->st);
   };
   if (h->precision == LH_PREC_MIXED) run(0.0f);
   else run(0.0);

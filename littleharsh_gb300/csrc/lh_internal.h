@@ -98,7 +98,8 @@ struct ProdArgs {
   int chunk;
 };
 template <typename R>
-void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const double2* rtw, cudaStream_t st);
+void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const FftPlan& pf, const double2* rtw,
+                  cudaStream_t st);
 
 template <typename R>
 struct MaskArgs {

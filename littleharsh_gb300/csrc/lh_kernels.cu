@@ -182,13 +182,66 @@ __device__ void x_forward_packed(int nr, cpx_t<R>* F, int hp, cpx_t<R>* const* r
   __syncthreads();
 }
 
+// Two real rows through one complex transform of length ngx (n): the inverse
+// takes the mixed rows A, B (nkx modes, zero beyond, imaginary part of the
+// kx = 0 mode dropped as the real inverse does) as z = a + i b; the forward
+// splits the transform of z = a + i b into the two half spectra.  This costs
+// fewer FP64 instructions than two half-length real transforms with their
+// pre/post twiddle passes.
 template <typename R>
-__global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph, const double2* __restrict__ rtw) {
+__device__ void x_inverse_pair(const cpx_t<R>* rowA, const cpx_t<R>* rowB, cpx_t<R>* F, R* outA, R* outB,
+                               const Dims& d, const FftPlan& pf) {
+  using T2 = cpx_t<R>;
+  const int n = d.ngx, nkx = d.nkx;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    T2 z = T2{0, 0};
+    if (k == 0) {
+      z = T2{rowA[0].x, rowB[0].x};
+    } else if (k < nkx) {
+      const T2 a = rowA[k], b = rowB[k];
+      z = T2{a.x - b.y, a.y + b.x};
+    } else if (k > n - nkx) {
+      const T2 a = rowA[n - k], b = rowB[n - k];
+      z = T2{a.x + b.y, b.x - a.y};
+    }
+    F[pf.perm[k]] = z;
+  }
+  __syncthreads();
+  fft_dit<R, +1, false>(F, 1, 1, n, pf, false);
+  for (int x = threadIdx.x; x < n; x += blockDim.x) {
+    const T2 z = F[x];
+    outA[x] = z.x;
+    outB[x] = z.y;
+  }
+  __syncthreads();
+}
+
+// Forward transform of np2 packed pairs F[p*n + perm[x]] = a[x] + i b[x]
+// into 2*np2 mixed rows (kx < nkx, scaled by 1/ngx).
+template <typename R>
+__device__ void x_forward_pairs(int np2, cpx_t<R>* F, cpx_t<R>* const* rows, const Dims& d, const FftPlan& pf) {
+  using T2 = cpx_t<R>;
+  const int n = d.ngx, nkx = d.nkx;
+  const R sc = (R)(0.5 / n);
+  fft_dit<R, -1, false>(F, np2, 1, n, pf, false);
+  for (int e = threadIdx.x; e < np2 * nkx; e += blockDim.x) {
+    const int p = e / nkx, k = e - p * nkx;
+    const T2 zk = F[p * n + k];
+    const T2 zc = F[p * n + ((n - k) % n)];
+    rows[2 * p][k] = T2{sc * (zk.x + zc.x), sc * (zk.y - zc.y)};
+    rows[2 * p + 1][k] = T2{sc * (zk.y + zc.y), sc * (zc.x - zk.x)};
+  }
+  __syncthreads();
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph, FftPlan pf,
+                                               const double2* __restrict__ rtw) {
   using T2 = cpx_t<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ngx = d.ngx, h = ngx / 2, hp = h + 1;
-  T2* F = reinterpret_cast<T2*>(smraw);       // 6 vectors of hp
-  R* rowsm = reinterpret_cast<R*>(F + 6 * hp);  // 6 rows of ngx
+  T2* F = reinterpret_cast<T2*>(smraw);             // 3 vectors of ngx (also holds the half-length v transform)
+  R* rowsm = reinterpret_cast<R*>(F + 3 * ngx);     // 6 rows of ngx
   R* up = rowsm;
   R* wp = rowsm + ngx;
   R* vp = rowsm + 2 * ngx;
@@ -204,61 +257,53 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
   double cmax = 0.0;
   // warm-up: previous centre and face
   if (c0 - 1 >= 1) {
-    const T2* rows[3] = {a.mu + (size_t)(c0 - 1) * d.mp + rowoff, a.mw + (size_t)(c0 - 1) * d.mp + rowoff,
-                         a.mv + (size_t)(c0 - 1) * d.mp + rowoff};
-    R* outs[3] = {up, wp, vp};
-    x_inverse<R>(rows, 3, F, hp, outs, d, ph, rtw);
+    x_inverse_pair<R>(a.mu + (size_t)(c0 - 1) * d.mp + rowoff, a.mw + (size_t)(c0 - 1) * d.mp + rowoff, F, up, wp, d,
+                      pf);
+    const T2* rows[1] = {a.mv + (size_t)(c0 - 1) * d.mp + rowoff};
+    R* outs[1] = {vp};
+    x_inverse<R>(rows, 1, F, hp, outs, d, ph, rtw);
   } else {
     for (int x = threadIdx.x; x < 3 * ngx; x += blockDim.x) up[x] = (R)0;
     __syncthreads();
   }
   for (int jj = c0; jj <= c1; ++jj) {
     const bool vface = jj <= d.nyv - 2;  // face jj interior (else the top wall, v = 0)
-    {
-      const T2* rows[3] = {a.mu + (size_t)jj * d.mp + rowoff, a.mw + (size_t)jj * d.mp + rowoff,
-                           a.mv + (size_t)jj * d.mp + rowoff};
-      R* outs[3] = {uc, wc, vc};
-      if (!vface)
-        for (int x = threadIdx.x; x < ngx; x += blockDim.x) vc[x] = (R)0;
-      x_inverse<R>(rows, vface ? 3 : 2, F, hp, outs, d, ph, rtw);
+    x_inverse_pair<R>(a.mu + (size_t)jj * d.mp + rowoff, a.mw + (size_t)jj * d.mp + rowoff, F, uc, wc, d, pf);
+    if (vface) {
+      const T2* rows[1] = {a.mv + (size_t)jj * d.mp + rowoff};
+      R* outs[1] = {vc};
+      x_inverse<R>(rows, 1, F, hp, outs, d, ph, rtw);
+    } else {
+      for (int x = threadIdx.x; x < ngx; x += blockDim.x) vc[x] = (R)0;
+      __syncthreads();
     }
     const bool fprod = jj - 1 >= 1;  // face jj-1 interior
     const R wcj = (R)a.wc[jj];
     const R wfj = fprod ? (R)a.wf[jj - 1] : (R)0;
     const double dyi = a.dyc[jj];
-    for (int m = threadIdx.x; m < h; m += blockDim.x) {
-      R q[6][2];
-#pragma unroll
-      for (int e = 0; e < 2; ++e) {
-        const int x = 2 * m + e;
-        const R u = uc[x], w = wc[x];
-        const R v = vp[x] + wcj * (vc[x] - vp[x]);
-        q[0][e] = u * u;
-        q[1][e] = u * w;
-        q[2][e] = w * w;
-        q[3][e] = v * v;
-        if (fprod) {
-          const R uf = up[x] + wfj * (u - up[x]);
-          const R wf = wp[x] + wfj * (w - wp[x]);
-          q[4][e] = uf * vp[x];
-          q[5][e] = wf * vp[x];
-        }
-        if (a.want_cfl) {
-          const double cv = fabs((double)u) * a.dxi + fabs((double)v) * dyi + fabs((double)w) * a.dzi;
-          cmax = fmax(cmax, cv);
-        }
+    // pairs: (uu, uw), (ww, vv) at centre jj; (uv, vw) at face jj-1
+    for (int x = threadIdx.x; x < ngx; x += blockDim.x) {
+      const R u = uc[x], w = wc[x];
+      const R v = vp[x] + wcj * (vc[x] - vp[x]);
+      const int px = pf.perm[x];
+      F[px] = T2{u * u, u * w};
+      F[ngx + px] = T2{w * w, v * v};
+      if (fprod) {
+        const R uf = up[x] + wfj * (u - up[x]);
+        const R wf = wp[x] + wfj * (w - wp[x]);
+        F[2 * ngx + px] = T2{uf * vp[x], wf * vp[x]};
       }
-      const int pm = ph.perm[m];
-#pragma unroll
-      for (int r = 0; r < 6; ++r)
-        if (r < 4 || fprod) F[r * hp + pm] = T2{q[r][0], q[r][1]};
+      if (a.want_cfl) {
+        const double cv = fabs((double)u) * a.dxi + fabs((double)v) * dyi + fabs((double)w) * a.dzi;
+        cmax = fmax(cmax, cv);
+      }
     }
     __syncthreads();
     {
       T2* rows[6] = {a.out[0] + (size_t)jj * d.mp + rowoff, a.out[1] + (size_t)jj * d.mp + rowoff,
                      a.out[2] + (size_t)jj * d.mp + rowoff, a.out[3] + (size_t)jj * d.mp + rowoff,
                      a.out[4] + (size_t)(jj - 1) * d.mp + rowoff, a.out[5] + (size_t)(jj - 1) * d.mp + rowoff};
-      x_forward_packed<R>(fprod ? 6 : 4, F, hp, rows, d, ph, rtw);
+      x_forward_pairs<R>(fprod ? 3 : 2, F, rows, d, pf);
     }
     // current becomes previous
     R* t;
@@ -279,13 +324,13 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
 }
 
 template <typename R>
-void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const double2* rtw, cudaStream_t st) {
+void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const FftPlan& pf, const double2* rtw,
+                  cudaStream_t st) {
   const int ncent = d.nyu - 2;
   if (ncent <= 0) return;
   dim3 grid(d.ngz, (ncent + a.chunk - 1) / a.chunk);
-  const int hp = d.ngx / 2 + 1;
-  size_t sm = sizeof(cpx_t<R>) * 6 * (size_t)hp + sizeof(R) * 6 * (size_t)d.ngx;
-  k_xprod<R><<<grid, 256, sm, st>>>(a, d, ph, rtw);
+  size_t sm = sizeof(cpx_t<R>) * 3 * (size_t)d.ngx + sizeof(R) * 6 * (size_t)d.ngx;
+  k_xprod<R><<<grid, 256, sm, st>>>(a, d, ph, pf, rtw);
 }
 
 // Canopy forcing on one mixed row of one processed plane: x-inverse, solid
@@ -304,12 +349,20 @@ __global__ void __launch_bounds__(128) k_xmask(MaskArgs<R> a, Dims d, FftPlan ph
   size_t plane = (size_t)blockIdx.y;
   T2* row = a.mix + plane * d.mp + (size_t)kz * d.nkx;
   const int tip = a.tipslot[f][pl];
+  const uint8_t* msk = a.mask[f] + ((size_t)pl * d.ngz + kz) * ngx;
+  // a row without solid points is unchanged by the forcing: its x round trip only drops the imaginary
+  // part of its kx = 0 value (the real inverse ignores it), so that is all it needs
+  int any = 0;
+  for (int x = threadIdx.x; x < ngx; x += blockDim.x) any |= msk[x];
+  if (!__syncthreads_or(any)) {
+    if (threadIdx.x == 0) row[0].y = (R)0;
+    return;
+  }
   {
     const T2* rows[2] = {row, tip >= 0 ? a.lymix + (size_t)tip * d.mp + (size_t)kz * d.nkx : row};
     R* outs[2] = {rr, ll};
     x_inverse<R>(rows, tip >= 0 ? 2 : 1, F, hp, outs, d, ph, rtw);
   }
-  const uint8_t* msk = a.mask[f] + ((size_t)pl * d.ngz + kz) * ngx;
   const R mb = (R)(-a.beta);
   for (int m = threadIdx.x; m < h; m += blockDim.x) {
     R v[2];
@@ -936,8 +989,10 @@ template void launch_zinv<double>(const ZJobs<double>&, const Dims&, const FftPl
 template void launch_zinv<float>(const ZJobs<float>&, const Dims&, const FftPlan&, int, cudaStream_t);
 template void launch_zfwd<double>(const ZJobs<double>&, const Dims&, const FftPlan&, int, double, cudaStream_t);
 template void launch_zfwd<float>(const ZJobs<float>&, const Dims&, const FftPlan&, int, double, cudaStream_t);
-template void launch_xprod<double>(const ProdArgs<double>&, const Dims&, const FftPlan&, const double2*, cudaStream_t);
-template void launch_xprod<float>(const ProdArgs<float>&, const Dims&, const FftPlan&, const double2*, cudaStream_t);
+template void launch_xprod<double>(const ProdArgs<double>&, const Dims&, const FftPlan&, const FftPlan&, const double2*,
+                                   cudaStream_t);
+template void launch_xprod<float>(const ProdArgs<float>&, const Dims&, const FftPlan&, const FftPlan&, const double2*,
+                                  cudaStream_t);
 template void launch_xmask<double>(const MaskArgs<double>&, const Dims&, const FftPlan&, const double2*, cudaStream_t);
 template void launch_xmask<float>(const MaskArgs<float>&, const Dims&, const FftPlan&, const double2*, cudaStream_t);
 
