@@ -31,17 +31,12 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+from littleharsh_gb300.workloads import CONFIG1, CONFIG2, MID288, ensemble_configs  # noqa: E402
+
 WORKLOADS = {
-    "config2_576x576x450_fp64": dict(Re=10000.0, alp=1.0, bet=2.0, ngalx=576, ngalz=576, ny=385, dyq=13.6, ppp=5,
-                                     geometry_type=3, posth=0.1, dsty=32, dstx=8, dstz=8, ntilex=48, ntilez=24,
-                                     flag_ctpress=0),
-    "config1_96x96x130_fp64": dict(Re=2800.0, alp=1.0, bet=2.0, ngalx=96, ngalz=96, ny=97, dyq=13.6, ppp=5,
-                                   geometry_type=3, posth=0.2, dsty=16, dstx=2, dstz=4, ntilex=12, ntilez=6,
-                                   flag_ctpress=0),
-    # mid-size case for ncu captures: inputs of the x pass larger than L2, ~2 GB on the device
-    "mid_288x288x226_fp64": dict(Re=5000.0, alp=1.0, bet=2.0, ngalx=288, ngalz=288, ny=193, dyq=13.6, ppp=5,
-                                 geometry_type=3, posth=0.1, dsty=16, dstx=4, dstz=4, ntilex=24, ntilez=12,
-                                 flag_ctpress=0),
+    "config2_576x576x450_fp64": CONFIG2,
+    "config1_96x96x130_fp64": CONFIG1,
+    "mid_288x288x226_fp64": MID288,
 }
 DEFAULT_WORKLOAD = "config2_576x576x450_fp64"
 METRIC = "grid-pt RK3 steps/s"
@@ -51,11 +46,12 @@ BYTES_PER_POINT_FP64 = 576  # compulsory state traffic per spectral point per RK
 
 def _peaks() -> dict:
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    out = {"hbm_gbs": 6800.0, "src": "fallback"}
+    out = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "src": "fallback"}
     if os.path.exists(p):
         try:
             d = json.load(open(p))
-            out = {"hbm_gbs": float(d["hbm_gbs"]), "src": "measured"}
+            out = {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d.get("bf16_tflops", 1900.0)),
+                   "src": "measured"}
         except Exception:
             pass
     # FP64 FMA peak of this machine's GB300 (own probe: 8 independent FMA chains per
@@ -241,22 +237,6 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
-def ensemble_configs():
-    """Configuration 4: 16 replicas of uneven sizes, canopy pitches pi/6, pi/8,
-    pi/12 (12x6, 16x8, 24x12 tiles), heights 0.1/0.2, Re_b 2800-6900
-    (Re_tau ~180-395), posts a quarter of the pitch wide."""
-    sizes = [(144, 129, 12)] * 6 + [(192, 193, 16)] * 6 + [(288, 257, 24)] * 4
-    tiles = [(12, 6), (16, 8), (24, 12)]
-    res = [2800.0, 4500.0, 6900.0]
-    out = []
-    for i, (ng, ny, dsty) in enumerate(sizes):
-        tx, tz = tiles[i % 3]
-        out.append(dict(Re=res[i % 3], alp=1.0, bet=2.0, ngalx=ng, ngalz=ng, ny=ny, dyq=13.6, ppp=5, geometry_type=3,
-                        posth=(0.1, 0.2)[i % 2], dsty=dsty, dstx=max(1, ng // tx // 4), dstz=max(1, ng // tz // 4),
-                        ntilex=tx, ntilez=tz, flag_ctpress=0))
-    return out
-
-
 def run_ensemble(args, rank: int, world: int):
     import littleharsh_gb300 as lh
     cfgs = ensemble_configs()
@@ -397,6 +377,71 @@ def run_ours(args, rank: int, world: int, local_rank: int, dist):
     s.close()
 
 
+def srnet_flops(Y: int, Z: int, X: int, train: bool) -> float:
+    """Tensor FLOPs of one forward (or forward + backward) of the network on a volume:
+    2 * 27 * cin * cout per voxel and convolution; the backward adds the data
+    gradient of every convolution but the first and the weight gradient of all."""
+    from littleharsh_gb300.srnet import layer_shapes
+    v = Y * Z * X
+    f = sum(2 * 27 * ci * co for ci, co in layer_shapes()) * v
+    if not train:
+        return float(f)
+    dgrad = sum(2 * 27 * ci * co for ci, co in layer_shapes()[1:]) * v
+    return float(f + dgrad + f)
+
+
+def run_srnet(args):
+    """The super-resolution network's kernels: a training step on configuration 1's
+    volume and inference on configuration 5's fine volume, CUDA events around
+    each, bf16 tensor-core FLOP rates against the measured bf16 peak."""
+    import torch
+    from littleharsh_gb300 import warmstart as ws
+    from littleharsh_gb300.srnet import SRNet
+    from littleharsh_gb300.workloads import CONFIG1, CONFIG5_FINE
+    peaks = _peaks()
+    net = SRNet(seed=0)
+    out = {"metric": "SR network bf16 TFLOP/s", "unit": "TFLOP/s", "higher_is_better": True, "n_gpus": 1,
+           "dtype": "bf16 (fp32 accumulate)", "kernel": "mma.sync m16n8k16 implicit-GEMM 3x3x3 conv"}
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    for name, cfg, train in (("train_step_config1", CONFIG1, True), ("inference_config5_fine", CONFIG5_FINE, False)):
+        gi = ws.GridInfo.from_config(cfg)
+        Y, Z, X = gi.nyu, gi.ngz, gi.ngx
+        g = torch.Generator(device="cuda").manual_seed(0)
+        x = torch.randn((Y, Z, X, 16), device="cuda", generator=g).to(torch.bfloat16)
+        base = torch.randn((Y * Z * X, 3), device="cuda", generator=g)
+        tgt = torch.randn((Y * Z * X, 3), device="cuda", generator=g)
+        loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+
+        def step():
+            if train:
+                net.zero_grad()
+                corr = net.forward(x, keep=True)
+                net.backward(net.loss_grad(corr, base, tgt, loss))
+                net.adam_step()
+            else:
+                net.forward(x)
+        for _ in range(max(args.warmup, 1)):
+            step()
+        torch.cuda.synchronize()
+        a, b = ev(), ev()
+        n = max(args.steps, 1)
+        a.record()
+        for _ in range(n):
+            step()
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / n
+        fl = srnet_flops(Y, Z, X, train)
+        tf = fl / (ms * 1e-3) / 1e12
+        out[name] = {"volume": [Y, Z, X], "ms": ms, "tflops": tf, "flops": fl,
+                     "frac_of_bf16_peak": tf / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None}
+        del x, base, tgt
+        torch.cuda.empty_cache()
+    out["value"] = out["train_step_config1"]["tflops"]
+    out["peak_bf16_tflops"] = peaks.get("bf16_tflops")
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -407,6 +452,7 @@ def main():
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ensemble", action="store_true", help="configuration 4: 16 replicas in one graph per step")
+    ap.add_argument("--srnet", action="store_true", help="the warm start's network kernels (training and inference)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -426,7 +472,9 @@ def main():
             torch.cuda.set_device(0)
         except Exception:
             pass
-    if args.ensemble:
+    if args.srnet:
+        run_srnet(args)
+    elif args.ensemble:
         run_ensemble(args, rank, world)
     else:
         run_ours(args, rank, world, local_rank, dist)

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "liblh_gb300.so")
-SOURCES = ["lh_kernels.cu", "lh_capi.cu", "lh_host.cpp", "lh_noalloc.cu", "lh_io.cpp"]
+SOURCES = ["lh_kernels.cu", "lh_capi.cu", "lh_host.cpp", "lh_noalloc.cu", "lh_io.cpp", "lh_srnet.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -31,7 +31,7 @@ def _needs_build() -> bool:
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "littleharsh.h")]
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
     return any(os.path.getmtime(p) > t for p in deps if os.path.exists(p))
 
 

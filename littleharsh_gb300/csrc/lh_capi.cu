@@ -82,6 +82,7 @@ struct lh_handle {
   bool have_fields = false, have_dt = false;
   long long iter = 0;
   cudaGraphExec_t graph = nullptr;
+  unsigned long long graph_gen = 0;  // bumped whenever captured launch arguments (dt) change
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0;
   int launches_per_step = 0;
@@ -813,6 +814,7 @@ int lh_set_time(lh_handle* h, double t, double dt, double mpgx, double QxT) {
     h->dt = dt;
     h->have_dt = true;
     if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    ++h->graph_gen;
     int rc = build_dt_tables(h);
     if (rc) return rc;
   }
@@ -884,6 +886,7 @@ struct lh_ensemble {
   int device = 0;
   cudaStream_t origin = nullptr;
   cudaGraphExec_t graph = nullptr;
+  std::vector<unsigned long long> gens;  // members' graph_gen at capture
   std::vector<cudaEvent_t> ev;  // fork event, then one join event per member
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   double last_ms = 0;
@@ -952,6 +955,13 @@ int lh_ensemble_step(lh_ensemble* e, int32_t nsteps, double* ms) {
   for (lh_handle* h : e->hs)
     if (!h->have_fields || !h->have_dt) return ens_fail(e, LH_ESTATE, "every member needs fields and dt");
   cudaSetDevice(e->device);
+  // a member whose dt changed since the capture has new launch arguments: capture again
+  bool stale = e->gens.size() != e->hs.size();
+  for (size_t i = 0; !stale && i < e->hs.size(); ++i) stale = e->gens[i] != e->hs[i]->graph_gen;
+  if (e->graph && stale) {
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
   if (!e->graph) {
     cudaGraph_t g = nullptr;
     cudaError_t ce = cudaStreamBeginCapture(e->origin, cudaStreamCaptureModeThreadLocal);
@@ -974,6 +984,8 @@ int lh_ensemble_step(lh_ensemble* e, int32_t nsteps, double* ms) {
     ce = cudaGraphInstantiate(&e->graph, g, 0);
     cudaGraphDestroy(g);
     if (ce != cudaSuccess) { e->graph = nullptr; return ens_fail(e, LH_ECUDA, "instantiate", ce); }
+    e->gens.clear();
+    for (lh_handle* h : e->hs) e->gens.push_back(h->graph_gen);
   }
   cudaEventRecord(e->t0, e->origin);
   for (int n = 0; n < nsteps; ++n) {

@@ -1,0 +1,495 @@
+// lh_srnet.cu -- BF16 tensor-core kernels of the super-resolution network
+// that lifts a coarse-grid field onto the fine grid (the learned warm start).
+//
+// The reference has no counterpart: its only initial conditions are a restart
+// file or a parabolic profile (start.f90:1488-1784).
+//
+// Activations are channels-last volumes [y][z][x][c] in bf16 with c = 16 or
+// 32; x and z are periodic (the Fourier directions of the channel), y is
+// zero-padded.  A 3x3x3 convolution is an implicit GEMM: rows = voxels,
+// columns = output channels, reduction = 27 taps x input channels, computed
+// with mma.sync m16n8k16 (bf16 in, fp32 accumulate).  A CTA stages a tile of
+// 8 z-rows x 32 x-voxels of one y level plus its halo (3 y levels x 10 z-rows
+// x 34 x-voxels) in shared memory with cp.async; the weights of the layer
+// stay in shared memory while the persistent CTA walks over tiles.  Fragments
+// come from shared memory with ldmatrix (the tap shift is just a different
+// row address).  Rows are padded by 16 bytes so the 8 row addresses of an
+// ldmatrix fall in distinct bank groups.
+//
+// Backward:
+//   data gradient = the forward kernel run on the output gradient with the
+//     taps mirrored and the channel roles swapped (lh_sr_flip_weights);
+//   weight gradient: rows = output channels, columns = input channels,
+//     reduction = voxels, one warp per 3 taps, accumulated in registers over
+//     all tiles of the persistent CTA and added to the fp32 gradient once.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lh_internal.h"
+#include "lh_srnet.h"
+#include "littleharsh.h"
+
+namespace lh {
+namespace sr {
+
+constexpr int TX = 32;            // x-voxels per tile (two m16 tiles)
+constexpr int TZ = 8;             // z-rows per tile (one warp each in the forward kernel)
+constexpr int HX = TX + 2, HZ = TZ + 2;
+constexpr int HROWS = 3 * HZ * HX;  // staged input rows (voxels) per tile
+
+struct Vol {
+  int X, Y, Z;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
+  // src-size 0 fills the 16 bytes with zeros and reads nothing
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_u32(dst)), "l"(src),
+               "r"(valid ? 16 : 0));
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(smem_u32(p)));
+}
+__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const void* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(smem_u32(p)));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Stage the input halo of tile (y, z0, x0) into sIn: rows [dy][zz][xx], each C
+// channels, row stride C + 8 elements.
+template <int C>
+__device__ __forceinline__ void stage_halo(__nv_bfloat16* sIn, const __nv_bfloat16* __restrict__ in, const Vol v,
+                                           int y, int z0, int x0) {
+  constexpr int CH = C / 8;  // 16-byte chunks per row
+  constexpr int RS = C + 8;
+  for (int c = threadIdx.x; c < HROWS * CH; c += blockDim.x) {
+    const int row = c / CH, part = c - row * CH;
+    const int xx = row % HX, zz = (row / HX) % HZ, dy = row / (HX * HZ);
+    const int gy = y + dy - 1;
+    const bool ok = gy >= 0 && gy < v.Y;
+    const int gz = (z0 + zz - 1 + v.Z) % v.Z, gx = (x0 + xx - 1 + v.X) % v.X;
+    const size_t vox = ok ? ((size_t)gy * v.Z + gz) * v.X + gx : 0;
+    cp_async16(sIn + (size_t)row * RS + part * 8, in + vox * C + part * 8, ok);
+  }
+}
+
+enum : int { EPI_RELU = 1, EPI_RES = 2, EPI_GATE = 4, EPI_BIAS = 8 };
+
+template <typename T> __device__ __forceinline__ void store2(T* p, float a, float b);
+template <> __device__ __forceinline__ void store2<float>(float* p, float a, float b) {
+  *reinterpret_cast<float2*>(p) = make_float2(a, b);
+}
+template <> __device__ __forceinline__ void store2<__nv_bfloat16>(__nv_bfloat16* p, float a, float b) {
+  *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(a, b);
+}
+
+// out[v][co] = epi( sum_tap sum_ci W[tap][co][ci] in[nbr(v, tap)][ci] )
+// epi: + bias, ReLU, zero where gate <= 0, + res (in this order, each optional)
+template <int CIN, int COUT, typename OutT>
+__global__ void __launch_bounds__(TZ * 32, 1)
+    k_conv_fwd(const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ w,
+               const float* __restrict__ bias, OutT* __restrict__ out, const __nv_bfloat16* __restrict__ res,
+               const __nv_bfloat16* __restrict__ gate, int epi, Vol v) {
+  constexpr int RSI = CIN + 8, RSW = CIN + 8;
+  constexpr int NT = COUT / 8;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __nv_bfloat16* sW = reinterpret_cast<__nv_bfloat16*>(smem_raw);
+  __nv_bfloat16* sIn = sW + 27 * COUT * RSW;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+  // weights [27][COUT][CIN] -> rows of RSW
+  for (int c = threadIdx.x; c < 27 * COUT * (CIN / 8); c += blockDim.x) {
+    const int row = c / (CIN / 8), part = c - row * (CIN / 8);
+    cp_async16(sW + (size_t)row * RSW + part * 8, w + (size_t)row * CIN + part * 8, true);
+  }
+  const int ntx = v.X / TX, ntz = v.Z / TZ;
+  const int ntiles = v.Y * ntz * ntx;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int xt = tile % ntx, rest = tile / ntx, zt = rest % ntz, y = rest / ntz;
+    const int x0 = xt * TX, z0 = zt * TZ;
+    __syncthreads();  // the previous tile's fragments have been read
+    stage_halo<CIN>(sIn, in, v, y, z0, x0);
+    cp_async_wait_all();
+    __syncthreads();
+
+    float acc[2][NT][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int j = 0; j < NT; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[mt][j][q] = 0.f;
+
+    const int zr = warp;
+    const int arow = (lane & 7) + ((lane >> 3) & 1) * 8;  // A: row within the m16 tile
+    const int acol = (lane >> 4) * 8;                      // A: k offset
+    const int bn = (lane >> 4) * 8 + (lane & 7);           // B: n within a pair of n8 tiles
+    const int bk = ((lane >> 3) & 1) * 8;                  // B: k offset
+#pragma unroll 1
+    for (int tap = 0; tap < 27; ++tap) {
+      const int dy = tap / 9, dz = (tap / 3) % 3, dx = tap % 3;
+      const __nv_bfloat16* rowbase = sIn + (size_t)((dy * HZ + zr + dz) * HX + dx) * RSI;
+      const __nv_bfloat16* wbase = sW + (size_t)tap * COUT * RSW;
+#pragma unroll
+      for (int kc = 0; kc < CIN / 16; ++kc) {
+        uint32_t a[2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) ldsm_x4(a[mt], rowbase + (size_t)(mt * 16 + arow) * RSI + kc * 16 + acol);
+#pragma unroll
+        for (int j = 0; j < NT; j += 2) {
+          uint32_t b[4];
+          ldsm_x4(b, wbase + (size_t)(j * 8 + bn) * RSW + kc * 16 + bk);
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt) {
+            mma_bf16(acc[mt][j], a[mt], b[0], b[1]);
+            mma_bf16(acc[mt][j + 1], a[mt], b[2], b[3]);
+          }
+        }
+      }
+    }
+    // epilogue
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int x = x0 + mt * 16 + g + half * 8;
+        const size_t vox = ((size_t)y * v.Z + z0 + zr) * v.X + x;
+#pragma unroll
+        for (int j = 0; j < NT; ++j) {
+          const int n = j * 8 + 2 * t;
+          float r0 = acc[mt][j][2 * half], r1 = acc[mt][j][2 * half + 1];
+          if (epi & EPI_BIAS) { r0 += bias[n]; r1 += bias[n + 1]; }
+          if (epi & EPI_RELU) { r0 = fmaxf(r0, 0.f); r1 = fmaxf(r1, 0.f); }
+          if (epi & EPI_GATE) {
+            const __nv_bfloat162 gv = *reinterpret_cast<const __nv_bfloat162*>(gate + vox * COUT + n);
+            if (!(__low2float(gv) > 0.f)) r0 = 0.f;
+            if (!(__high2float(gv) > 0.f)) r1 = 0.f;
+          }
+          if (epi & EPI_RES) {
+            const __nv_bfloat162 rv = *reinterpret_cast<const __nv_bfloat162*>(res + vox * COUT + n);
+            r0 += __low2float(rv);
+            r1 += __high2float(rv);
+          }
+          store2<OutT>(out + vox * COUT + n, r0, r1);
+        }
+      }
+  }
+  cp_async_wait_all();  // a CTA without a tile still drains its weight copies
+}
+
+// dW[tap][co][ci] += sum_v dout[v][co] in[nbr(v, tap)][ci]; db[co] += sum_v dout[v][co].
+// Warp w owns taps 3w .. 3w+2 (9 warps); M = output channels (m16 tiles),
+// N = input channels (n8 tiles), K = the tile's voxels, 16 at a time.
+constexpr int WG_WARPS = 9;
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(WG_WARPS * 32, 1)
+    k_conv_wgrad(const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ dout,
+                 float* __restrict__ dw, float* __restrict__ db, Vol v) {
+  constexpr int RSI = CIN + 8, RSD = COUT + 8;
+  constexpr int MT = COUT / 16, NT = CIN / 8;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __nv_bfloat16* sIn = reinterpret_cast<__nv_bfloat16*>(smem_raw);
+  __nv_bfloat16* sD = sIn + (size_t)HROWS * RSI;
+  float* sBias = reinterpret_cast<float*>(sD + (size_t)TZ * TX * RSD);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < COUT; i += blockDim.x) sBias[i] = 0.f;
+
+  float acc[3][MT][NT][4];
+#pragma unroll
+  for (int q = 0; q < 3; ++q)
+#pragma unroll
+    for (int m = 0; m < MT; ++m)
+#pragma unroll
+      for (int j = 0; j < NT; ++j)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[q][m][j][e] = 0.f;
+  float bacc = 0.f;  // thread < COUT: its channel's bias gradient
+
+  const int ntx = v.X / TX, ntz = v.Z / TZ;
+  const int ntiles = v.Y * ntz * ntx;
+  // ldmatrix.trans row addresses: matrix q = lane / 8, row r = lane % 8
+  const int qd = lane >> 3, r8 = lane & 7;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int xt = tile % ntx, rest = tile / ntx, zt = rest % ntz, y = rest / ntz;
+    const int x0 = xt * TX, z0 = zt * TZ;
+    __syncthreads();
+    stage_halo<CIN>(sIn, in, v, y, z0, x0);
+    for (int c = threadIdx.x; c < TZ * TX * (COUT / 8); c += blockDim.x) {
+      const int row = c / (COUT / 8), part = c - row * (COUT / 8);
+      const int xx = row % TX, zz = row / TX;
+      const size_t vox = ((size_t)y * v.Z + z0 + zz) * v.X + x0 + xx;
+      cp_async16(sD + (size_t)row * RSD + part * 8, dout + vox * COUT + part * 8, true);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (threadIdx.x < COUT) {
+      float s = 0.f;
+      for (int r = 0; r < TZ * TX; ++r) s += __bfloat162float(sD[(size_t)r * RSD + threadIdx.x]);
+      bacc += s;
+    }
+#pragma unroll 1
+    for (int ks = 0; ks < TZ * 2; ++ks) {
+      const int zr = ks >> 1, xh = (ks & 1) * 16;
+      // A = dout^T: stored rows = voxels (k), columns = channels (m)
+      uint32_t a[MT][4];
+#pragma unroll
+      for (int m = 0; m < MT; ++m) {
+        const int vrow = zr * TX + xh + (qd >> 1) * 8 + r8;
+        ldsm_x4_t(a[m], sD + (size_t)vrow * RSD + m * 16 + (qd & 1) * 8);
+      }
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const int tap = warp * 3 + q;
+        const int dy = tap / 9, dz = (tap / 3) % 3, dx = tap % 3;
+        const int hrow = (dy * HZ + zr + dz) * HX + dx + xh + (qd & 1) * 8 + r8;
+#pragma unroll
+        for (int j = 0; j < NT; j += 2) {
+          uint32_t b[4];
+          ldsm_x4_t(b, sIn + (size_t)hrow * RSI + (j + (qd >> 1)) * 8);
+#pragma unroll
+          for (int m = 0; m < MT; ++m) {
+            mma_bf16(acc[q][m][j], a[m], b[0], b[1]);
+            mma_bf16(acc[q][m][j + 1], a[m], b[2], b[3]);
+          }
+        }
+      }
+    }
+  }
+  cp_async_wait_all();
+  const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const int tap = warp * 3 + q;
+#pragma unroll
+    for (int m = 0; m < MT; ++m)
+#pragma unroll
+      for (int j = 0; j < NT; ++j)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int co = m * 16 + g + (e >> 1) * 8, ci = j * 8 + 2 * t + (e & 1);
+          atomicAdd(dw + ((size_t)tap * COUT + co) * CIN + ci, acc[q][m][j][e]);
+        }
+  }
+  if (threadIdx.x < COUT) atomicAdd(db + threadIdx.x, bacc);
+}
+
+// wt[tap'][ci][co] = w[26 - tap'][co][ci]: the data gradient of a convolution
+// is the convolution of the output gradient with the mirrored, transposed taps
+__global__ void k_flip_weights(const __nv_bfloat16* __restrict__ w, __nv_bfloat16* __restrict__ wt, int cin,
+                               int cout) {
+  const int n = 27 * cin * cout;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int co = i % cout, rest = i / cout, ci = rest % cin, tap = rest / cin;
+    wt[i] = w[((size_t)(26 - tap) * cout + co) * cin + ci];
+  }
+}
+
+// Loss of one sample: pred = base + corr (channels 0..2 of the network's fp32
+// output, 16 channels per voxel), L = sum (pred - target)^2 / (3 nvox);
+// dcorr = dL/dcorr in bf16 with channels 3..15 zero.  `loss` gets L added.
+__global__ void k_mse(const float* __restrict__ corr, const float* __restrict__ base,
+                      const float* __restrict__ target, __nv_bfloat16* __restrict__ dcorr, double* __restrict__ loss,
+                      long long nvox, float scale) {
+  __shared__ float red[32];
+  float s = 0.f;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nvox; v += (long long)gridDim.x * blockDim.x) {
+    float d[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      d[c] = base[v * 3 + c] + corr[v * 16 + c] - target[v * 3 + c];
+      s += d[c] * d[c];
+    }
+    const __nv_bfloat162 o0 = __floats2bfloat162_rn(scale * 2.f * d[0], scale * 2.f * d[1]);
+    const __nv_bfloat162 o1 = __floats2bfloat162_rn(scale * 2.f * d[2], 0.f);
+    uint4 w0;
+    w0.x = *reinterpret_cast<const uint32_t*>(&o0);
+    w0.y = *reinterpret_cast<const uint32_t*>(&o1);
+    w0.z = 0u;
+    w0.w = 0u;
+    uint4* dst = reinterpret_cast<uint4*>(dcorr + v * 16);
+    dst[0] = w0;
+    dst[1] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (threadIdx.x == 0) atomicAdd(loss, (double)s * (double)scale);
+  }
+}
+
+// AdamW on fp32 master parameters; the bf16 copy the convolutions read is
+// refreshed in the same pass.  bc1/bc2 are the bias corrections 1 - beta^t.
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, __nv_bfloat16* __restrict__ pb, int n, float lr, float b1, float b2,
+                       float eps, float wd, float bc1, float bc2) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float mh = mi / bc1, vh = vi / bc2;
+    const float pi = p[i] * (1.f - lr * wd) - lr * mh / (sqrtf(vh) + eps);
+    p[i] = pi;
+    if (pb) pb[i] = __float2bfloat16_rn(pi);
+  }
+}
+
+// ---- launchers ---------------------------------------------------------------
+
+template <int CIN, int COUT>
+constexpr size_t fwd_smem() {
+  return (size_t)(27 * COUT * (CIN + 8) + HROWS * (CIN + 8)) * 2;
+}
+template <int CIN, int COUT>
+constexpr size_t wgrad_smem() {
+  return (size_t)(HROWS * (CIN + 8) + TZ * TX * (COUT + 8)) * 2 + COUT * 4;
+}
+
+int num_sms() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
+}
+
+template <int CIN, int COUT, typename OutT>
+cudaError_t conv_fwd(const void* in, const void* w, const float* bias, void* out, const void* res, const void* gate,
+                     int epi, Vol v, cudaStream_t st) {
+  auto k = k_conv_fwd<CIN, COUT, OutT>;
+  const size_t sm = fwd_smem<CIN, COUT>();
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  const int ntiles = v.Y * (v.Z / TZ) * (v.X / TX);
+  const int grid = ntiles < num_sms() ? ntiles : num_sms();
+  k<<<grid, TZ * 32, sm, st>>>((const __nv_bfloat16*)in, (const __nv_bfloat16*)w, bias, (OutT*)out,
+                               (const __nv_bfloat16*)res, (const __nv_bfloat16*)gate, epi, v);
+  return cudaGetLastError();
+}
+
+template <int CIN, int COUT>
+cudaError_t conv_wgrad(const void* in, const void* dout, float* dw, float* db, Vol v, cudaStream_t st) {
+  auto k = k_conv_wgrad<CIN, COUT>;
+  const size_t sm = wgrad_smem<CIN, COUT>();
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  const int ntiles = v.Y * (v.Z / TZ) * (v.X / TX);
+  const int grid = ntiles < num_sms() ? ntiles : num_sms();
+  k<<<grid, WG_WARPS * 32, sm, st>>>((const __nv_bfloat16*)in, (const __nv_bfloat16*)dout, dw, db, v);
+  return cudaGetLastError();
+}
+
+}  // namespace sr
+}  // namespace lh
+
+// ---- C ABI (include/lh_srnet.h) ------------------------------------------------
+
+using lh::sr::Vol;
+
+namespace {
+int sr_check_vol(int X, int Y, int Z) {
+  if (X <= 0 || Y <= 0 || Z <= 0 || X % lh::sr::TX || Z % lh::sr::TZ) {
+    lh::set_init_error("lh_sr: volume needs X a multiple of 32 and Z a multiple of 8");
+    return LH_EINVAL;
+  }
+  return LH_OK;
+}
+int sr_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return LH_OK;
+  lh::set_init_error(cudaGetErrorString(e));
+  return LH_ECUDA;
+}
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+}  // namespace
+
+extern "C" {
+
+int lh_sr_conv_fwd(int32_t cin, int32_t cout, const void* in, const void* w, const float* bias, void* out,
+                   int32_t out_f32, const void* res, const void* gate, int32_t flags, int32_t X, int32_t Y, int32_t Z,
+                   void* stream) {
+  int rc = sr_check_vol(X, Y, Z);
+  if (rc) return rc;
+  if (!in || !w || !out || !aligned16(in) || !aligned16(w) || ((flags & 2) && !res) || ((flags & 4) && !gate) ||
+      ((flags & 8) && !bias)) {
+    lh::set_init_error("lh_sr_conv_fwd: missing or misaligned pointer");
+    return LH_EINVAL;
+  }
+  const Vol v{X, Y, Z};
+  cudaStream_t st = (cudaStream_t)stream;
+  using bf = __nv_bfloat16;
+  if (cin == 16 && cout == 32 && !out_f32) return sr_cuda(lh::sr::conv_fwd<16, 32, bf>(in, w, bias, out, res, gate, flags, v, st));
+  if (cin == 32 && cout == 32 && !out_f32) return sr_cuda(lh::sr::conv_fwd<32, 32, bf>(in, w, bias, out, res, gate, flags, v, st));
+  if (cin == 32 && cout == 16 && !out_f32) return sr_cuda(lh::sr::conv_fwd<32, 16, bf>(in, w, bias, out, res, gate, flags, v, st));
+  if (cin == 32 && cout == 16 && out_f32) return sr_cuda(lh::sr::conv_fwd<32, 16, float>(in, w, bias, out, res, gate, flags, v, st));
+  lh::set_init_error("lh_sr_conv_fwd: channel pair not built (16->32, 32->32, 32->16)");
+  return LH_EINVAL;
+}
+
+int lh_sr_conv_wgrad(int32_t cin, int32_t cout, const void* in, const void* dout, float* dw, float* db, int32_t X,
+                     int32_t Y, int32_t Z, void* stream) {
+  int rc = sr_check_vol(X, Y, Z);
+  if (rc) return rc;
+  if (!in || !dout || !dw || !db || !aligned16(in) || !aligned16(dout)) {
+    lh::set_init_error("lh_sr_conv_wgrad: missing or misaligned pointer");
+    return LH_EINVAL;
+  }
+  const Vol v{X, Y, Z};
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cin == 16 && cout == 32) return sr_cuda(lh::sr::conv_wgrad<16, 32>(in, dout, dw, db, v, st));
+  if (cin == 32 && cout == 32) return sr_cuda(lh::sr::conv_wgrad<32, 32>(in, dout, dw, db, v, st));
+  if (cin == 32 && cout == 16) return sr_cuda(lh::sr::conv_wgrad<32, 16>(in, dout, dw, db, v, st));
+  lh::set_init_error("lh_sr_conv_wgrad: channel pair not built (16->32, 32->32, 32->16)");
+  return LH_EINVAL;
+}
+
+int lh_sr_flip_weights(int32_t cin, int32_t cout, const void* w, void* wt, void* stream) {
+  if (!w || !wt || cin <= 0 || cout <= 0) return LH_EINVAL;
+  const int n = 27 * cin * cout;
+  lh::sr::k_flip_weights<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)w,
+                                                                          (__nv_bfloat16*)wt, cin, cout);
+  return sr_cuda(cudaGetLastError());
+}
+
+int lh_sr_mse(const float* corr, const float* base, const float* target, void* dcorr, double* loss, int64_t nvox,
+              void* stream) {
+  if (!corr || !base || !target || !dcorr || !loss || nvox <= 0 || !aligned16(dcorr)) return LH_EINVAL;
+  const int blocks = (int)((nvox + 255) / 256 < 4 * 1024 ? (nvox + 255) / 256 : 4 * 1024);
+  lh::sr::k_mse<<<blocks, 256, 0, (cudaStream_t)stream>>>(corr, base, target, (__nv_bfloat16*)dcorr, loss, nvox,
+                                                          1.0f / (3.0f * (float)nvox));
+  return sr_cuda(cudaGetLastError());
+}
+
+int lh_sr_adam(float* p, const float* g, float* m, float* v, void* p_bf16, int32_t n, float lr, float beta1,
+               float beta2, float eps, float weight_decay, int32_t step, void* stream) {
+  if (!p || !g || !m || !v || n <= 0 || step < 1) return LH_EINVAL;
+  const float bc1 = 1.f - powf(beta1, (float)step), bc2 = 1.f - powf(beta2, (float)step);
+  const int blocks = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
+  lh::sr::k_adam<<<blocks, 256, 0, (cudaStream_t)stream>>>(p, g, m, v, (__nv_bfloat16*)p_bf16, n, lr, beta1, beta2,
+                                                           eps, weight_decay, bc1, bc2);
+  return sr_cuda(cudaGetLastError());
+}
+
+}  // extern "C"

@@ -111,10 +111,14 @@ def test_canopy_lists_match_oracle_masks(lh, oracle_mod, cfg):
 
 
 def test_header_declares_exported_symbols(lh):
-    """Every lh_* function declared in include/littleharsh.h is exported by the library."""
+    """Every lh_* function declared in include/*.h is exported by the library."""
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    hdr = open(os.path.join(root, "include", "littleharsh.h")).read()
-    declared = set(re.findall(r"^\s*(?:int|void|const char\s*\*)\s+(lh_[a-z0-9_]+)\s*\(", hdr, re.M))
+    inc = os.path.join(root, "include")
+    declared = set()
+    for f in sorted(os.listdir(inc)):
+        if f.endswith(".h"):
+            hdr = open(os.path.join(inc, f)).read()
+            declared |= set(re.findall(r"^\s*(?:int|void|const char\s*\*)\s+(lh_[a-z0-9_]+)\s*\(", hdr, re.M))
     assert declared == set(lh.EXPORTED_SYMBOLS)
     L = lh.load_library()
     for name in declared:
