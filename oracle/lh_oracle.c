@@ -375,6 +375,13 @@ struct lho {
   /* transforms */
   fftplan zplan;
   rfftplan xplan;
+  /* bands: resolution 1 is the middle band's (= resolution 0 without bands) */
+  int banded;
+  int ngx2, ngz2, nx2, nz2, nkx2;
+  fftplan zplan2;
+  rfftplan xplan2;
+  int N30, N31, N32, N33, N40, N41, N42, N43; /* N(3,0..3), N(4,0..3) */
+  uint8_t* lng;                               /* per mode of a plane: 1 = long column */
   /* statistics */
   int istat;
   double* stat;   /* 13 profiles */
@@ -387,7 +394,27 @@ struct lho {
 
 #define CIDX(s, jj, kk, ii) (2 * (((size_t)(jj) * (s)->nz + (kk)) * (s)->nkx + (ii)))
 
-static int kz_slot(const lho* s, int kk) { return kk < s->nz / 2 ? kk : kk + (s->ngz - s->nz); }
+/* Resolution of the physical plane of u level j / v level j: 0 wall bands, 1
+ * middle band (planelim, start.f90:1326-1378). */
+static int res_u(const lho* s, int j) { return s->banded && j > s->N41 && j <= s->N42; }
+static int res_v(const lho* s, int j) { return s->banded && j > s->N31 && j <= s->N32; }
+
+/* Where a column's y range puts level j (jlim, start.f90:1147-1175): 0 outside
+ * the column, 1 interior, 2 boundary row. */
+static int lev_u(const lho* s, int col, int j) {
+  if (!s->banded || s->lng[col]) return (j == s->ju0 || j == s->ju1) ? 2 : 1;
+  if (j == s->N40 || j == s->N41 + 1 || j == s->N42 || j == s->N43 + 1) return 2;
+  return ((j > s->N40 && j <= s->N41) || (j > s->N42 && j <= s->N43)) ? 1 : 0;
+}
+static int lev_v(const lho* s, int col, int j) {
+  if (!s->banded || s->lng[col]) return (j == s->jv0 || j == s->jv1) ? 2 : 1;
+  if (j == s->N30 || j == s->N31 + 1 || j == s->N32 || j == s->N33 + 1) return 2;
+  return ((j > s->N30 && j <= s->N31) || (j > s->N32 && j <= s->N33)) ? 1 : 0;
+}
+static int lev_p(const lho* s, int col, int j) {
+  if (!s->banded || s->lng[col]) return 1;
+  return ((j > s->N40 && j <= s->N41) || (j > s->N42 && j <= s->N43)) ? 1 : 0;
+}
 
 void lho_get_sizes(const lho* s, lho_sizes* out) { *out = s->sz; }
 
@@ -574,18 +601,31 @@ static int build_canopy(lho* s, char* err, int errlen) {
 
 
 /* LU_buildP + LU_decP (tridLU_3D_IB.f90:497-571,643-684) for every column. */
+/* The p-level index ranges (first, last) of column col's bands: one for a
+ * long column, band 1's and band 3's for a short one. */
+static void p_segments(const lho* s, int col, int segs[2][2], int* ns) {
+  if (!s->banded || s->lng[col]) {
+    segs[0][0] = 0; segs[0][1] = s->nyp - 1; *ns = 1;
+    return;
+  }
+  segs[0][0] = s->N40 + 1 - s->jp0; segs[0][1] = s->N41 - s->jp0;
+  segs[1][0] = s->N42 + 1 - s->jp0; segs[1][1] = s->N43 - s->jp0;
+  *ns = 2;
+}
+
+/* LU_buildP + LU_decP (tridLU_3D_IB.f90:497-571,643-684) per column and band. */
 static void build_dg(lho* s) {
   const int np = s->nyp, nc = s->nplane;
-  const int ns = s->jp0, ne = s->jp1;
   s->dg1 = (double*)xcalloc((size_t)np * nc, sizeof(double));
   s->dg2 = (double*)xcalloc((size_t)np * nc, sizeof(double));
   s->dg3 = (double*)xcalloc((size_t)np * nc, sizeof(double));
-  double* Db = (double*)xcalloc((size_t)np + 2, sizeof(double)); /* index j-(ns-1) */
+  const int p0 = s->jp0;
+  double* Db = (double*)xcalloc((size_t)np + 2, sizeof(double)); /* index j-(p0-1) */
   double* Gb = (double*)xcalloc((size_t)np + 2, sizeof(double));
   double* Dt = (double*)xcalloc((size_t)np + 2, sizeof(double));
   double* Gt = (double*)xcalloc((size_t)np + 2, sizeof(double));
-#define IX(j) ((j) - (ns - 1))
-  for (int j = ns; j <= ne; ++j) {
+#define IX(j) ((j) - (p0 - 1))
+  for (int j = p0; j <= s->jp1; ++j) {
     Db[IX(j - 1)] = -s->ddthetavi * DTHU(s, j);
     Gb[IX(j)] = -s->ddthetavi * DTHV(s, j);
     Dt[IX(j)] = s->ddthetavi * DTHU(s, j);
@@ -596,27 +636,32 @@ static void build_dg(lho* s) {
   for (int col = 0; col < nc; ++col) {
     const int kk = col / s->nkx, i = col % s->nkx;
     const double k2x = s->k2x[i], k2z = s->k2z[kk];
-#define A1(j) s->dg1[(size_t)((j) - ns) * nc + col]
-#define A2(j) s->dg2[(size_t)((j) - ns) * nc + col]
-#define A3(j) s->dg3[(size_t)((j) - ns) * nc + col]
-    A2(ns) = (Dt[IX(ns)] * Gb[IX(ns)]) + k2x + k2z;
-    A3(ns) = (Dt[IX(ns)] * Gt[IX(ns + 1)]);
-    A2(ne) = (Db[IX(ne - 1)] * Gt[IX(ne)]) + k2x + k2z;
-    A1(ne) = (Db[IX(ne - 1)] * Gb[IX(ne - 1)]);
-    for (int j = ns + 1; j <= ne - 1; ++j) {
-      A2(j) = (Db[IX(j - 1)] * Gt[IX(j)]) + (Dt[IX(j)] * Gb[IX(j)]) + k2x + k2z;
-      A1(j) = (Db[IX(j - 1)] * Gb[IX(j - 1)]);
-      A3(j) = (Dt[IX(j)] * Gt[IX(j + 1)]);
-    }
-    if (col == 0) { /* mode (0,0): Dirichlet row for psi (tridLU_3D_IB.f90:548-554) */
-      A1(ns) = 0.0;
-      A2(ns) = pin;
-      A3(ns) = 0.0;
-    }
-    A2(ns) = 1.0 / A2(ns);
-    for (int j = ns + 1; j <= ne; ++j) {
-      A3(j - 1) = A3(j - 1) * A2(j - 1);
-      A2(j) = 1.0 / (A2(j) - A1(j) * A3(j - 1));
+    int segs[2][2], nsg;
+    p_segments(s, col, segs, &nsg);
+#define A1(j) s->dg1[(size_t)((j) - p0) * nc + col]
+#define A2(j) s->dg2[(size_t)((j) - p0) * nc + col]
+#define A3(j) s->dg3[(size_t)((j) - p0) * nc + col]
+    for (int q = 0; q < nsg; ++q) {
+      const int ns = segs[q][0] + p0, ne = segs[q][1] + p0;
+      A2(ns) = (Dt[IX(ns)] * Gb[IX(ns)]) + k2x + k2z;
+      A3(ns) = (Dt[IX(ns)] * Gt[IX(ns + 1)]);
+      A2(ne) = (Db[IX(ne - 1)] * Gt[IX(ne)]) + k2x + k2z;
+      A1(ne) = (Db[IX(ne - 1)] * Gb[IX(ne - 1)]);
+      for (int j = ns + 1; j <= ne - 1; ++j) {
+        A2(j) = (Db[IX(j - 1)] * Gt[IX(j)]) + (Dt[IX(j)] * Gb[IX(j)]) + k2x + k2z;
+        A1(j) = (Db[IX(j - 1)] * Gb[IX(j - 1)]);
+        A3(j) = (Dt[IX(j)] * Gt[IX(j + 1)]);
+      }
+      if (col == 0) { /* mode (0,0), a long column: Dirichlet row for psi (tridLU_3D_IB.f90:548-554) */
+        A1(ns) = 0.0;
+        A2(ns) = pin;
+        A3(ns) = 0.0;
+      }
+      A2(ns) = 1.0 / A2(ns);
+      for (int j = ns + 1; j <= ne; ++j) {
+        A3(j - 1) = A3(j - 1) * A2(j - 1);
+        A2(j) = 1.0 / (A2(j) - A1(j) * A3(j - 1));
+      }
     }
 #undef A1
 #undef A2
@@ -637,6 +682,9 @@ void lho_destroy(lho* s) {
   for (size_t i = 0; i < sizeof f / sizeof f[0]; ++i) free(f[i]);
   fft_plan_free(&s->zplan);
   rfft_plan_free(&s->xplan);
+  fft_plan_free(&s->zplan2);
+  rfft_plan_free(&s->xplan2);
+  free(s->lng);
   free(s);
 }
 
@@ -671,9 +719,26 @@ lho* lho_create(const lho_config* cfg, char* err, int errlen) {
   else { snprintf(err, (size_t)errlen, "only geometry types 0 and 3 have a forcing builder"); lho_destroy(s); return NULL; }
   s->dny = cfg->dsty;
   if (s->dny < 0) { snprintf(err, (size_t)errlen, "dsty < 0"); lho_destroy(s); return NULL; }
+  /* bands (start.f90:95-118): the middle band's resolution */
+  s->ngx2 = cfg->ngalx2 > 0 ? cfg->ngalx2 : s->ngx;
+  s->ngz2 = cfg->ngalz2 > 0 ? cfg->ngalz2 : s->ngz;
+  s->banded = (s->ngx2 != s->ngx || s->ngz2 != s->ngz);
+  s->nx2 = 2 * (s->ngx2 / 3); s->nz2 = 2 * (s->ngz2 / 3); s->nkx2 = s->nx2 / 2 + 1;
+  if (s->ngx2 > s->ngx || s->ngz2 > s->ngz || s->ngx2 < 6 || s->ngz2 < 6) {
+    snprintf(err, (size_t)errlen, "the middle band must not be finer than the wall bands"); lho_destroy(s); return NULL;
+  }
+  if (fft_plan_init(&s->zplan2, s->ngz2) || rfft_plan_init(&s->xplan2, s->ngx2)) {
+    snprintf(err, (size_t)errlen, "Ngal must factor into 2, 3 and 4"); lho_destroy(s); return NULL;
+  }
+  s->lng = (uint8_t*)xcalloc((size_t)s->nplane, 1);
+  for (int kk = 0; kk < s->nz; ++kk)
+    for (int i = 0; i < s->nkx; ++i) {
+      const int kz = kk < s->nz / 2 ? kk : kk - s->nz; /* signed kz index */
+      s->lng[(size_t)kk * s->nkx + i] = (i < s->nkx2 && kz >= -s->nz2 / 2 && kz < s->nz2 / 2);
+    }
   int N[4][5] = {{0}}, Ngal[4][5] = {{0}};
-  Ngal[0][1] = cfg->ngalx; Ngal[0][2] = cfg->ngalx; Ngal[0][3] = cfg->ngalx; Ngal[0][4] = -2;
-  Ngal[1][1] = cfg->ngalz; Ngal[1][2] = cfg->ngalz; Ngal[1][3] = cfg->ngalz; Ngal[1][4] = 0;
+  Ngal[0][1] = cfg->ngalx; Ngal[0][2] = s->ngx2; Ngal[0][3] = cfg->ngalx; Ngal[0][4] = -2;
+  Ngal[1][1] = cfg->ngalz; Ngal[1][2] = s->ngz2; Ngal[1][3] = cfg->ngalz; Ngal[1][4] = 0;
   Ngal[2][3] = cfg->ny - 2;
   memcpy(N, Ngal, sizeof N);
   for (int b = 1; b <= 3; ++b) { N[0][b] = 2 * (Ngal[0][b] / 3); N[1][b] = 2 * (Ngal[1][b] / 3); }
@@ -681,6 +746,8 @@ lho* lho_create(const lho_config* cfg, char* err, int errlen) {
   build_grid(s, cfg->ny, cfg->dyq, cfg->ppp, posth, h_ny1, N, Ngal);
   memcpy(s->sz.N, N, sizeof N);
   memcpy(s->sz.Ngal, Ngal, sizeof Ngal);
+  s->N30 = N[2][0]; s->N31 = N[2][1]; s->N32 = N[2][2]; s->N33 = N[2][3];
+  s->N40 = N[3][0]; s->N41 = N[3][1]; s->N42 = N[3][2]; s->N43 = N[3][3];
   s->ju0 = N[3][0]; s->ju1 = N[3][3] + 1;
   s->jv0 = N[2][0]; s->jv1 = N[2][3] + 1;
   s->jp0 = N[3][0] + 1; s->jp1 = N[3][3];
@@ -720,6 +787,10 @@ lho* lho_create(const lho_config* cfg, char* err, int errlen) {
   z->ju0 = s->ju0; z->ju1 = s->ju1; z->jv0 = s->jv0; z->jv1 = s->jv1; z->jp0 = s->jp0; z->jp1 = s->jp1;
   z->nyu = s->nyu; z->nyv = s->nyv; z->nyp = s->nyp; z->nn = s->nn; z->dny = s->dny;
   if (build_canopy(s, err, errlen)) { lho_destroy(s); return NULL; }
+  for (int q = 0; q < s->nibu; ++q)
+    if (res_u(s, s->ibu_j[q])) { snprintf(err, (size_t)errlen, "canopy planes must lie in the wall bands"); lho_destroy(s); return NULL; }
+  for (int q = 0; q < s->nibv; ++q)
+    if (res_v(s, s->ibv_j[q])) { snprintf(err, (size_t)errlen, "canopy planes must lie in the wall bands"); lho_destroy(s); return NULL; }
   z->nibu_planes = s->nibu; z->nibv_planes = s->nibv;
   /* fields */
   const size_t fu = 2 * (size_t)s->nyu * s->nplane, fv = 2 * (size_t)s->nyv * s->nplane, fp = 2 * (size_t)s->nyp * s->nplane;
@@ -831,8 +902,15 @@ static size_t plane_scratch_len(const lho* s) {
   return 2 * (size_t)s->ngz * s->nkx + 4 * (size_t)s->ngz + (size_t)s->ngx + 2 + 2 * (size_t)s->ngx + 4;
 }
 
-static void plane_to_phys_(const lho* s, const double* spec, double* phys, double* scr) {
-  const int ngz = s->ngz, nkx = s->nkx, ngx = s->ngx, nz = s->nz;
+/* Plane transforms at resolution r (0: wall bands, 1: middle band).  The
+ * spectral plane always holds the fine mode set; resolution 1 reads and writes
+ * only the long modes (kz mapped between the two FFT orders) and zeroes the
+ * others on the way back. */
+static void plane_to_phys_r(const lho* s, int r, const double* spec, double* phys, double* scr) {
+  const int ngz = r ? s->ngz2 : s->ngz, nkx = r ? s->nkx2 : s->nkx, ngx = r ? s->ngx2 : s->ngx;
+  const int nz = r ? s->nz2 : s->nz, pitch = s->nkx;
+  const fftplan* zp = r ? &s->zplan2 : &s->zplan;
+  const rfftplan* xp = r ? &s->xplan2 : &s->xplan;
   double* tmp = scr;
   double* col = tmp + 2 * (size_t)ngz * nkx;
   double* fsc = col + 2 * ngz;
@@ -841,11 +919,12 @@ static void plane_to_phys_(const lho* s, const double* spec, double* phys, doubl
   for (int i = 0; i < nkx; ++i) {
     memset(col, 0, sizeof(double) * 2 * ngz);
     for (int kk = 0; kk < nz; ++kk) {
-      int sl = kz_slot(s, kk);
-      col[2 * sl] = spec[2 * ((size_t)kk * nkx + i)];
-      col[2 * sl + 1] = spec[2 * ((size_t)kk * nkx + i) + 1];
+      const int sl = kk < nz / 2 ? kk : kk + (ngz - nz);
+      const int ks = kk < nz / 2 ? kk : kk - nz + s->nz; /* row of the fine mode set */
+      col[2 * sl] = spec[2 * ((size_t)ks * pitch + i)];
+      col[2 * sl + 1] = spec[2 * ((size_t)ks * pitch + i) + 1];
     }
-    fft_rec_(&s->zplan, ngz, 1, col, 1, fsc, +1, 0);
+    fft_rec_(zp, ngz, 1, col, 1, fsc, +1, 0);
     for (int k = 0; k < ngz; ++k) {
       tmp[2 * ((size_t)k * nkx + i)] = fsc[2 * k];
       tmp[2 * ((size_t)k * nkx + i) + 1] = fsc[2 * k + 1];
@@ -854,20 +933,24 @@ static void plane_to_phys_(const lho* s, const double* spec, double* phys, doubl
   for (int k = 0; k < ngz; ++k) {
     memset(X, 0, sizeof(double) * (size_t)(ngx + 2));
     memcpy(X, tmp + 2 * (size_t)k * nkx, sizeof(double) * 2 * nkx);
-    rfft_inv(&s->xplan, X, phys + (size_t)k * ngx, rsc);
+    rfft_inv(xp, X, phys + (size_t)k * ngx, rsc);
   }
 }
 
-static void plane_to_spec_(const lho* s, const double* phys, double* spec, double* scr) {
-  const int ngz = s->ngz, nkx = s->nkx, ngx = s->ngx, nz = s->nz;
+static void plane_to_spec_r(const lho* s, int r, const double* phys, double* spec, double* scr) {
+  const int ngz = r ? s->ngz2 : s->ngz, nkx = r ? s->nkx2 : s->nkx, ngx = r ? s->ngx2 : s->ngx;
+  const int nz = r ? s->nz2 : s->nz, pitch = s->nkx;
+  const fftplan* zp = r ? &s->zplan2 : &s->zplan;
+  const rfftplan* xp = r ? &s->xplan2 : &s->xplan;
   double* tmp = scr;
   double* col = tmp + 2 * (size_t)ngz * nkx;
   double* fsc = col + 2 * ngz;
   double* X = fsc + 2 * ngz;
   double* rsc = X + ngx + 2;
   const double dnx = 1.0 / ngx, dnz = 1.0 / ngz;
+  if (r) memset(spec, 0, sizeof(double) * 2 * (size_t)s->nz * pitch);
   for (int k = 0; k < ngz; ++k) {
-    rfft_fwd(&s->xplan, phys + (size_t)k * ngx, X, rsc);
+    rfft_fwd(xp, phys + (size_t)k * ngx, X, rsc);
     for (int m = 0; m < nkx; ++m) {
       tmp[2 * ((size_t)k * nkx + m)] = dnx * X[2 * m];
       tmp[2 * ((size_t)k * nkx + m) + 1] = dnx * X[2 * m + 1];
@@ -879,13 +962,21 @@ static void plane_to_spec_(const lho* s, const double* phys, double* spec, doubl
       col[2 * k] = tmp[2 * ((size_t)k * nkx + i)];
       col[2 * k + 1] = tmp[2 * ((size_t)k * nkx + i) + 1];
     }
-    fft_rec_(&s->zplan, ngz, 1, col, 1, fsc, -1, 0);
+    fft_rec_(zp, ngz, 1, col, 1, fsc, -1, 0);
     for (int kk = 0; kk < nz; ++kk) {
-      int sl = kz_slot(s, kk);
-      spec[2 * ((size_t)kk * nkx + i)] = dnz * fsc[2 * sl];
-      spec[2 * ((size_t)kk * nkx + i) + 1] = dnz * fsc[2 * sl + 1];
+      const int sl = kk < nz / 2 ? kk : kk + (ngz - nz);
+      const int ks = kk < nz / 2 ? kk : kk - nz + s->nz;
+      spec[2 * ((size_t)ks * pitch + i)] = dnz * fsc[2 * sl];
+      spec[2 * ((size_t)ks * pitch + i) + 1] = dnz * fsc[2 * sl + 1];
     }
   }
+}
+
+static void plane_to_phys_(const lho* s, const double* spec, double* phys, double* scr) {
+  plane_to_phys_r(s, 0, spec, phys, scr);
+}
+static void plane_to_spec_(const lho* s, const double* phys, double* spec, double* scr) {
+  plane_to_spec_r(s, 0, phys, spec, scr);
 }
 
 void lho_plane_to_phys(const lho* s, const double* spec, double* phys) {
@@ -919,6 +1010,11 @@ static void rhs0(lho* s, int k) {
       const double k2 = s->k2x[i] + s->k2z[kk];
       const size_t c0 = 2 * ((size_t)jj * nc + col), cm = c0 - 2 * (size_t)nc, cp = c0 + 2 * (size_t)nc;
       const size_t pc = 2 * ((size_t)jp * nc + col);
+      if (lev_u(s, col, j) != 1) { /* outside a short column, or its end row */
+        s->r1[c0] = s->r1[c0 + 1] = s->r3[c0] = s->r3[c0 + 1] = 0.0;
+        s->ly1[c0] = s->ly1[c0 + 1] = s->ly3[c0] = s->ly3[c0 + 1] = 0.0;
+        continue;
+      }
       for (int f = 0; f < 2; ++f) {
         const double* u = f == 0 ? s->u1 : s->u3;
         const double* nu = f == 0 ? s->nu1 : s->nu3;
@@ -951,6 +1047,10 @@ static void rhs0(lho* s, int k) {
       const double k2 = s->k2x[i] + s->k2z[kk];
       const size_t c0 = 2 * ((size_t)jj * nc + col), cm = c0 - 2 * (size_t)nc, cp = c0 + 2 * (size_t)nc;
       const size_t p0 = 2 * ((size_t)jp * nc + col), p1 = p0 + 2 * (size_t)nc;
+      if (lev_v(s, col, j) != 1) {
+        s->r2[c0] = s->r2[c0 + 1] = s->ly2[c0] = s->ly2[c0 + 1] = 0.0;
+        continue;
+      }
       for (int c = 0; c < 2; ++c) {
         double L = a1 * s->u2[cm + c] + (k2 + a2) * s->u2[c0 + c] + a3 * s->u2[cp + c];
         s->ly2[c0 + c] = a1 * s->u2[cm + c] + (a2) * s->u2[c0 + c] + a3 * s->u2[cp + c];
@@ -967,25 +1067,33 @@ static void rhs0(lho* s, int k) {
  * substage and r -= gamma*Nu.  If cflmax != NULL it receives
  * max(|u|/dx + |v|/dy + |w|/dz) over the interior centres. */
 static void nonlinear(lho* s, int k, double* cflmax) {
-  const int ngx = s->ngx, ngz = s->ngz, nc = s->nplane, nkx = s->nkx;
-  const size_t PL = (size_t)ngx * ngz;
-  double* Uc = (double*)xcalloc(PL * s->nyu, 8);
-  double* Wc = (double*)xcalloc(PL * s->nyu, 8);
-  double* Vf = (double*)xcalloc(PL * s->nyv, 8);
+  const int nc = s->nplane, nkx = s->nkx;
+  const int nres = s->banded ? 2 : 1;
+  /* physical planes of every level at each resolution in use */
+  double *Uc[2] = {NULL, NULL}, *Wc[2] = {NULL, NULL}, *Vf[2] = {NULL, NULL};
+  size_t PLr[2];
+  for (int r = 0; r < nres; ++r) {
+    PLr[r] = (size_t)(r ? s->ngx2 : s->ngx) * (r ? s->ngz2 : s->ngz);
+    Uc[r] = (double*)xcalloc(PLr[r] * s->nyu, 8);
+    Wc[r] = (double*)xcalloc(PLr[r] * s->nyu, 8);
+    Vf[r] = (double*)xcalloc(PLr[r] * s->nyv, 8);
+  }
+  const size_t PL = PLr[0];
   const size_t sl = plane_scratch_len(s);
 #pragma omp parallel
   {
     double* scr = (double*)xcalloc(sl, 8);
+    for (int r = 0; r < nres; ++r) {
 #pragma omp for schedule(dynamic)
-    for (int jj = 1; jj < s->nyu - 1; ++jj) {
-      plane_to_phys_(s, s->u1 + 2 * (size_t)jj * nc, Uc + PL * jj, scr);
-      plane_to_phys_(s, s->u3 + 2 * (size_t)jj * nc, Wc + PL * jj, scr);
+      for (int jj = 1; jj < s->nyu - 1; ++jj) {
+        plane_to_phys_r(s, r, s->u1 + 2 * (size_t)jj * nc, Uc[r] + PLr[r] * jj, scr);
+        plane_to_phys_r(s, r, s->u3 + 2 * (size_t)jj * nc, Wc[r] + PLr[r] * jj, scr);
+      }
+#pragma omp for schedule(dynamic)
+      for (int jj = 1; jj < s->nyv - 1; ++jj) plane_to_phys_r(s, r, s->u2 + 2 * (size_t)jj * nc, Vf[r] + PLr[r] * jj, scr);
     }
-#pragma omp for schedule(dynamic)
-    for (int jj = 1; jj < s->nyv - 1; ++jj) plane_to_phys_(s, s->u2 + 2 * (size_t)jj * nc, Vf + PL * jj, scr);
     free(scr);
   }
-  const double dxi = ngx / s->Lx, dzi = ngz / s->Lz;
   double cmax = 0.0;
 #pragma omp parallel reduction(max : cmax)
   {
@@ -994,47 +1102,52 @@ static void nonlinear(lho* s, int k, double* cflmax) {
 #pragma omp for schedule(dynamic)
     for (int jj = 1; jj < s->nyu - 1; ++jj) {
       const int j = jj + s->ju0;
+      const int r = res_u(s, j);   /* each centre plane at its band's resolution */
+      const size_t P = PLr[r];
+      const double dxi = (r ? s->ngx2 : s->ngx) / s->Lx, dzi = (r ? s->ngz2 : s->ngz) / s->Lz;
       const int fv = j - s->jv0; /* face j lives at v index fv, face j-1 at fv-1 */
       const double wc = (YU(s, j) - YV(s, j - 1)) / (YV(s, j) - YV(s, j - 1));
       const double dyi = 1.0 / (YV(s, j) - YV(s, j - 1));
-      const double* U = Uc + PL * jj; const double* W = Wc + PL * jj;
-      const double* V0 = Vf + PL * (fv - 1); const double* V1 = Vf + PL * fv;
-      for (size_t n = 0; n < PL; ++n) {
+      const double* U = Uc[r] + P * jj; const double* W = Wc[r] + P * jj;
+      const double* V0 = Vf[r] + P * (fv - 1); const double* V1 = Vf[r] + P * fv;
+      for (size_t n = 0; n < P; ++n) {
         const double v = V0[n] + wc * (V1[n] - V0[n]);
         q[n] = U[n] * U[n];
-        q[PL + n] = U[n] * W[n];
-        q[2 * PL + n] = W[n] * W[n];
-        q[3 * PL + n] = v * v;
+        q[P + n] = U[n] * W[n];
+        q[2 * P + n] = W[n] * W[n];
+        q[3 * P + n] = v * v;
         if (cflmax) {
           double cv = fabs(U[n]) * dxi + fabs(v) * dyi + fabs(W[n]) * dzi;
           if (cv > cmax) cmax = cv;
         }
       }
-      plane_to_spec_(s, q, s->pUU + 2 * (size_t)jj * nc, scr);
-      plane_to_spec_(s, q + PL, s->pUW + 2 * (size_t)jj * nc, scr);
-      plane_to_spec_(s, q + 2 * PL, s->pWW + 2 * (size_t)jj * nc, scr);
-      plane_to_spec_(s, q + 3 * PL, s->pVV + 2 * (size_t)jj * nc, scr);
+      plane_to_spec_r(s, r, q, s->pUU + 2 * (size_t)jj * nc, scr);
+      plane_to_spec_r(s, r, q + P, s->pUW + 2 * (size_t)jj * nc, scr);
+      plane_to_spec_r(s, r, q + 2 * P, s->pWW + 2 * (size_t)jj * nc, scr);
+      plane_to_spec_r(s, r, q + 3 * P, s->pVV + 2 * (size_t)jj * nc, scr);
     }
 #pragma omp for schedule(dynamic)
     for (int jj = 1; jj < s->nyv - 1; ++jj) {
       const int j = jj + s->jv0;
+      const int r = res_v(s, j);   /* each face plane at its band's resolution */
+      const size_t P = PLr[r];
       const int cu = j - s->ju0; /* centre j and j+1 */
       const double wf = (YV(s, j) - YU(s, j)) / (YU(s, j + 1) - YU(s, j));
-      const double* U0 = Uc + PL * cu; const double* U1 = Uc + PL * (cu + 1);
-      const double* W0 = Wc + PL * cu; const double* W1 = Wc + PL * (cu + 1);
-      const double* V = Vf + PL * jj;
-      for (size_t n = 0; n < PL; ++n) {
+      const double* U0 = Uc[r] + P * cu; const double* U1 = Uc[r] + P * (cu + 1);
+      const double* W0 = Wc[r] + P * cu; const double* W1 = Wc[r] + P * (cu + 1);
+      const double* V = Vf[r] + P * jj;
+      for (size_t n = 0; n < P; ++n) {
         const double u = U0[n] + wf * (U1[n] - U0[n]);
         const double w = W0[n] + wf * (W1[n] - W0[n]);
         q[n] = u * V[n];
-        q[PL + n] = w * V[n];
+        q[P + n] = w * V[n];
       }
-      plane_to_spec_(s, q, s->pUV + 2 * (size_t)jj * nc, scr);
-      plane_to_spec_(s, q + PL, s->pVW + 2 * (size_t)jj * nc, scr);
+      plane_to_spec_r(s, r, q, s->pUV + 2 * (size_t)jj * nc, scr);
+      plane_to_spec_r(s, r, q + P, s->pVW + 2 * (size_t)jj * nc, scr);
     }
     free(scr); free(q);
   }
-  free(Uc); free(Wc); free(Vf);
+  for (int r = 0; r < nres; ++r) { free(Uc[r]); free(Wc[r]); free(Vf[r]); }
   if (cflmax) *cflmax = cmax;
   if (k < 0) return;
   /* wall faces carry v = 0: their products vanish */
@@ -1053,6 +1166,10 @@ static void nonlinear(lho* s, int k, double* cflmax) {
       const double kx = s->kx[i], kz = s->kz[kk];
       const size_t c0 = 2 * ((size_t)jj * nc + col);
       const size_t f1 = 2 * ((size_t)fv * nc + col), f0 = f1 - 2 * (size_t)nc;
+      if (lev_u(s, col, j) != 1) {
+        s->nu1[c0] = s->nu1[c0 + 1] = s->nu3[c0] = s->nu3[c0 + 1] = 0.0;
+        continue;
+      }
       for (int comp = 0; comp < 2; ++comp) {
         const double* A = comp == 0 ? s->pUU : s->pUW;
         const double* B = comp == 0 ? s->pUW : s->pWW;
@@ -1077,6 +1194,10 @@ static void nonlinear(lho* s, int k, double* cflmax) {
       const double kx = s->kx[i], kz = s->kz[kk];
       const size_t c0 = 2 * ((size_t)jj * nc + col);
       const size_t v0 = 2 * ((size_t)cu * nc + col), v1 = v0 + 2 * (size_t)nc;
+      if (lev_v(s, col, j) != 1) {
+        s->nu2[c0] = s->nu2[c0 + 1] = 0.0;
+        continue;
+      }
       const double nr = (-kx * s->pUV[c0 + 1] - kz * s->pVW[c0 + 1]) + c * (s->pVV[v1] - s->pVV[v0]);
       const double ni = (kx * s->pUV[c0] + kz * s->pVW[c0]) + c * (s->pVV[v1 + 1] - s->pVV[v0 + 1]);
       s->nu2[c0] = nr; s->nu2[c0 + 1] = ni;
@@ -1088,14 +1209,16 @@ static void nonlinear(lho* s, int k, double* cflmax) {
 
 /* solveU/solveV first half (littleharsh.f90:746-757,793-804) and the axz
  * division of LUsolU/LUsolV (tridLU_3D_IB.f90:90-98,165-173). */
-static void implicit_rhs(lho* s, double* r, const double* u, int ny, double beta) {
+static void implicit_rhs(lho* s, double* r, const double* u, int grid, double beta) {
   const int nc = s->nplane, nkx = s->nkx;
+  const int ny = grid == 0 ? s->nyu : s->nyv, j0 = grid == 0 ? s->ju0 : s->jv0;
   const double dt = s->dt;
 #pragma omp parallel for schedule(static)
   for (int jj = 0; jj < ny; ++jj) {
     for (int col = 0; col < nc; ++col) {
       const size_t c0 = 2 * ((size_t)jj * nc + col);
-      if (jj == 0 || jj == ny - 1) { r[c0] = 0.0; r[c0 + 1] = 0.0; continue; }
+      const int lv = grid == 0 ? lev_u(s, col, jj + j0) : lev_v(s, col, jj + j0);
+      if (lv != 1) { r[c0] = 0.0; r[c0 + 1] = 0.0; continue; }  /* boundary rows and outside short columns */
       const int kk = col / nkx, i = col % nkx;
       const double axz = 1.0 - beta * (s->k2x[i] + s->k2z[kk]);
       r[c0] = (u[c0] + dt * r[c0]) / axz;
@@ -1136,50 +1259,67 @@ static void immersed(lho* s, double* r, const double* ly, int grid, double beta)
   }
 }
 
-/* LU_build + LU_dec (tridLU_3D_IB.f90:427-493,601-640) for band 2, then the
- * Thomas sweeps of LUsolU/LUsolV (:106-116,179-189). */
+/* LU_build + LU_dec (tridLU_3D_IB.f90:427-493,601-640) of one band's column
+ * range jl..jh (global j) into a1..a3 (indexed by level), boundary rows with
+ * that band's gridweighting. */
+static void helm_lu(const lho* s, int grid, int band, int jl, int jh, double beta, double* a1, double* a2, double* a3) {
+  const int j0 = grid == 0 ? s->ju0 : s->jv0;
+  const int l = jl - j0, h = jh - j0;
+  for (int jj = l + 1; jj < h; ++jj) {
+    const int j = jj + j0;
+    a1[jj] = -beta * (grid == 0 ? D2U(s, 1, j) : D2V(s, 1, j));
+    a2[jj] = 1.0 - beta * (grid == 0 ? D2U(s, 2, j) : D2V(s, 2, j));
+    a3[jj] = -beta * (grid == 0 ? D2U(s, 3, j) : D2V(s, 3, j));
+  }
+  a1[l] = 0.0; a2[l] = 1.0; a3[l] = grid == 0 ? s->gw[band][0] : 0.0;
+  a1[h] = grid == 0 ? s->gw[band][1] : 0.0; a2[h] = 1.0; a3[h] = 0.0;
+  a2[l] = 1.0 / a2[l];
+  for (int jj = l + 1; jj <= h; ++jj) {
+    a3[jj - 1] = a3[jj - 1] * a2[jj - 1];
+    a2[jj] = 1.0 / (a2[jj] - a1[jj] * a3[jj - 1]);
+  }
+}
+
+/* The Thomas sweeps of LUsolU/LUsolV (tridLU_3D_IB.f90:106-116,179-189) per
+ * column over its bands: long columns over band 2's range, short columns over
+ * band 1's and band 3's ranges (zero outside them). */
 static void helmholtz(lho* s, double* x, int grid, double beta) {
   const int ny = grid == 0 ? s->nyu : s->nyv;
   const int j0 = grid == 0 ? s->ju0 : s->jv0;
-  double* a1 = (double*)xcalloc((size_t)ny, 8);
-  double* a2 = (double*)xcalloc((size_t)ny, 8);
-  double* a3 = (double*)xcalloc((size_t)ny, 8);
-  if (grid == 0) {
-    a1[0] = 0.0; a2[0] = 1.0; a3[0] = s->gw[1][0];
-    for (int jj = 1; jj < ny - 1; ++jj) {
-      int j = jj + j0;
-      a1[jj] = -beta * D2U(s, 1, j);
-      a2[jj] = 1.0 - beta * (D2U(s, 2, j));
-      a3[jj] = -beta * D2U(s, 3, j);
-    }
-    a1[ny - 1] = s->gw[1][1]; a2[ny - 1] = 1.0; a3[ny - 1] = 0.0;
-  } else {
-    a1[0] = 0.0; a2[0] = 1.0; a3[0] = 0.0;
-    for (int jj = 1; jj < ny - 1; ++jj) {
-      int j = jj + j0;
-      a1[jj] = -beta * D2V(s, 1, j);
-      a2[jj] = 1.0 - beta * (D2V(s, 2, j));
-      a3[jj] = -beta * D2V(s, 3, j);
-    }
-    a1[ny - 1] = 0.0; a2[ny - 1] = 1.0; a3[ny - 1] = 0.0;
-  }
-  a2[0] = 1.0 / a2[0];
-  for (int jj = 1; jj < ny; ++jj) {
-    a3[jj - 1] = a3[jj - 1] * a2[jj - 1];
-    a2[jj] = 1.0 / (a2[jj] - a1[jj] * a3[jj - 1]);
+  double* A = (double*)xcalloc((size_t)9 * ny, 8);  /* [band][3][ny] */
+  helm_lu(s, grid, 1, j0, j0 + ny - 1, beta, A + 3 * ny, A + 4 * ny, A + 5 * ny);
+  if (s->banded) {
+    const int b1 = grid == 0 ? s->N41 + 1 : s->N31 + 1, b3 = grid == 0 ? s->N42 : s->N32;
+    helm_lu(s, grid, 0, j0, b1, beta, A, A + ny, A + 2 * ny);
+    helm_lu(s, grid, 2, b3, j0 + ny - 1, beta, A + 6 * ny, A + 7 * ny, A + 8 * ny);
   }
   const int nc = s->nplane;
 #pragma omp parallel for schedule(static)
   for (int col = 0; col < nc; ++col) {
-    for (int c = 0; c < 2; ++c) {
+    int segs[2][3], ns = 0;  /* band, first, last level index */
+    if (!s->banded || s->lng[col]) {
+      segs[0][0] = 1; segs[0][1] = 0; segs[0][2] = ny - 1; ns = 1;
+    } else {
+      const int b1 = (grid == 0 ? s->N41 + 1 : s->N31 + 1) - j0, b3 = (grid == 0 ? s->N42 : s->N32) - j0;
+      segs[0][0] = 0; segs[0][1] = 0; segs[0][2] = b1;
+      segs[1][0] = 2; segs[1][1] = b3; segs[1][2] = ny - 1; ns = 2;
+      for (int jj = b1 + 1; jj < b3; ++jj) x[2 * ((size_t)jj * nc + col)] = x[2 * ((size_t)jj * nc + col) + 1] = 0.0;
+    }
+    for (int q = 0; q < ns; ++q) {
+      const double* a1 = A + (size_t)3 * segs[q][0] * ny;
+      const double* a2 = a1 + ny;
+      const double* a3 = a2 + ny;
+      const int l = segs[q][1], h = segs[q][2];
+      for (int c = 0; c < 2; ++c) {
 #define X(jj) x[2 * ((size_t)(jj) * nc + col) + c]
-      X(0) = X(0) * a2[0];
-      for (int jj = 1; jj < ny; ++jj) X(jj) = (X(jj) - a1[jj] * X(jj - 1)) * a2[jj];
-      for (int jj = ny - 2; jj >= 0; --jj) X(jj) = X(jj) - a3[jj] * X(jj + 1);
+        X(l) = X(l) * a2[l];
+        for (int jj = l + 1; jj <= h; ++jj) X(jj) = (X(jj) - a1[jj] * X(jj - 1)) * a2[jj];
+        for (int jj = h - 1; jj >= l; --jj) X(jj) = X(jj) - a3[jj] * X(jj + 1);
 #undef X
+      }
     }
   }
-  free(a1); free(a2); free(a3);
+  free(A);
 }
 
 void lho_tridiag_solve(int n, const double* b1, const double* b2, const double* b3, double* x) {
@@ -1245,6 +1385,7 @@ static void divergence(lho* s) {
       const double kx = s->kx[i], kz = s->kz[kk];
       const size_t cu = 2 * (ju * nc + col), cv = 2 * (jv * nc + col), cvm = cv - 2 * (size_t)nc;
       const size_t cd = 2 * ((size_t)jj * nc + col);
+      if (!lev_p(s, col, j)) { s->div[cd] = s->div[cd + 1] = 0.0; continue; }
       s->div[cd] = (-kx * s->u1[cu + 1] - kz * s->u3[cu + 1]) + c * (s->u2[cv] - s->u2[cvm]);
       s->div[cd + 1] = (kx * s->u1[cu] + kz * s->u3[cu]) + c * (s->u2[cv + 1] - s->u2[cvm + 1]);
     }
@@ -1262,14 +1403,19 @@ static void pressure_and_correct(lho* s, int k) {
   s->psi[0] = 0.0; s->psi[1] = 0.0; /* psi(0,0) at the first p point */
 #pragma omp parallel for schedule(static)
   for (int col = 0; col < nc; ++col) {
-    for (int c = 0; c < 2; ++c) {
+    int segs[2][2], ns;
+    p_segments(s, col, segs, &ns);
+    for (int q = 0; q < ns; ++q) {
+      const int l = segs[q][0], h = segs[q][1];
+      for (int c = 0; c < 2; ++c) {
 #define X(jj) s->psi[2 * ((size_t)(jj) * nc + col) + c]
 #define A(a, jj) s->a[(size_t)(jj) * nc + col]
-      X(0) = X(0) * A(dg2, 0);
-      for (int jj = 1; jj < np; ++jj) X(jj) = (X(jj) - A(dg1, jj) * X(jj - 1)) * A(dg2, jj);
-      for (int jj = np - 2; jj >= 0; --jj) X(jj) = X(jj) - A(dg3, jj) * X(jj + 1);
+        X(l) = X(l) * A(dg2, l);
+        for (int jj = l + 1; jj <= h; ++jj) X(jj) = (X(jj) - A(dg1, jj) * X(jj - 1)) * A(dg2, jj);
+        for (int jj = h - 1; jj >= l; --jj) X(jj) = X(jj) - A(dg3, jj) * X(jj + 1);
 #undef X
 #undef A
+      }
     }
   }
   for (size_t n = 0; n < 2 * (size_t)np * nc; ++n) s->p[n] = s->p[n] + s->psi[n];
@@ -1282,6 +1428,7 @@ static void pressure_and_correct(lho* s, int k) {
     const double kx = dtrk * s->kx[i], kz = dtrk * s->kz[kk];
     for (int jj = 1; jj < s->nyu - 1; ++jj) {
       const int j = jj + s->ju0;
+      if (lev_u(s, col, j) != 1) continue;
       const size_t cu = 2 * ((size_t)jj * nc + col), cp = 2 * ((size_t)(j - s->jp0) * nc + col);
       /* u -= (i kx dtrk) psi */
       s->u1[cu] = s->u1[cu] - (-kx * s->psi[cp + 1]);
@@ -1292,6 +1439,11 @@ static void pressure_and_correct(lho* s, int k) {
     for (int jj = 1; jj < s->nyv - 1; ++jj) {
       const int j = jj + s->jv0;
       const size_t cv = 2 * ((size_t)jj * nc + col), cp = 2 * ((size_t)(j - s->jp0) * nc + col), cp1 = cp + 2 * (size_t)nc;
+      const int lv = lev_v(s, col, j);
+      if (lv != 1) {  /* v = 0 on the ends of a short column's bands (v_corr, littleharsh.f90:904-905) */
+        if (lv == 2) s->u2[cv] = s->u2[cv + 1] = 0.0;
+        continue;
+      }
       const double f = dtrk_u2 * DTHV(s, j);
       s->u2[cv] = s->u2[cv] - f * (s->psi[cp1] - s->psi[cp]);
       s->u2[cv + 1] = s->u2[cv + 1] - f * (s->psi[cp1 + 1] - s->psi[cp + 1]);
@@ -1318,9 +1470,9 @@ int lho_substage(lho* s, int krk, int upto) {
   const double beta = s->bRK[k] * s->dt / s->Re;
   rhs0(s, k);
   nonlinear(s, k, NULL);
-  implicit_rhs(s, s->r1, s->u1, s->nyu, beta);
-  implicit_rhs(s, s->r2, s->u2, s->nyv, beta);
-  implicit_rhs(s, s->r3, s->u3, s->nyu, beta);
+  implicit_rhs(s, s->r1, s->u1, 0, beta);
+  implicit_rhs(s, s->r2, s->u2, 1, beta);
+  implicit_rhs(s, s->r3, s->u3, 0, beta);
   if (upto <= 1) return 0;
   immersed(s, s->r1, s->ly1, 0, beta);
   immersed(s, s->r2, s->ly2, 1, beta);
@@ -1452,21 +1604,28 @@ void lho_stats_accumulate(lho* s) {
 #pragma omp for schedule(dynamic)
     for (int jj = 0; jj < L; ++jj) {
       double acc[13] = {0};
+      /* each plane summed over its band's physical points (stats.f90 loops over N(1:2,bandPL)) */
       if (jj < s->nyu) {
-        plane_to_phys_(s, s->u1 + 2 * (size_t)jj * nc, A, scr);
-        plane_to_phys_(s, vi + 2 * (size_t)jj * nc, B, scr);
-        for (size_t n = 0; n < PL; ++n) { acc[0] += A[n]; acc[1] += A[n] * A[n]; acc[8] += A[n] * B[n]; }
-        plane_to_phys_(s, s->u3 + 2 * (size_t)jj * nc, B, scr);
-        for (size_t n = 0; n < PL; ++n) { acc[4] += B[n]; acc[5] += B[n] * B[n]; acc[9] += A[n] * B[n]; }
+        const int r = res_u(s, jj + s->ju0);
+        const size_t P = r ? (size_t)s->ngx2 * s->ngz2 : PL;
+        plane_to_phys_r(s, r, s->u1 + 2 * (size_t)jj * nc, A, scr);
+        plane_to_phys_r(s, r, vi + 2 * (size_t)jj * nc, B, scr);
+        for (size_t n = 0; n < P; ++n) { acc[0] += A[n]; acc[1] += A[n] * A[n]; acc[8] += A[n] * B[n]; }
+        plane_to_phys_r(s, r, s->u3 + 2 * (size_t)jj * nc, B, scr);
+        for (size_t n = 0; n < P; ++n) { acc[4] += B[n]; acc[5] += B[n] * B[n]; acc[9] += A[n] * B[n]; }
       }
       if (jj < s->nyv) {
-        plane_to_phys_(s, s->u2 + 2 * (size_t)jj * nc, A, scr);
-        plane_to_phys_(s, wi + 2 * (size_t)jj * nc, B, scr);
-        for (size_t n = 0; n < PL; ++n) { acc[2] += A[n]; acc[3] += A[n] * A[n]; acc[10] += A[n] * B[n]; }
+        const int r = res_v(s, jj + s->jv0);
+        const size_t P = r ? (size_t)s->ngx2 * s->ngz2 : PL;
+        plane_to_phys_r(s, r, s->u2 + 2 * (size_t)jj * nc, A, scr);
+        plane_to_phys_r(s, r, wi + 2 * (size_t)jj * nc, B, scr);
+        for (size_t n = 0; n < P; ++n) { acc[2] += A[n]; acc[3] += A[n] * A[n]; acc[10] += A[n] * B[n]; }
       }
       if (jj < s->nyp) {
-        plane_to_phys_(s, s->p + 2 * (size_t)jj * nc, A, scr);
-        for (size_t n = 0; n < PL; ++n) { acc[6] += A[n]; acc[7] += A[n] * A[n]; }
+        const int r = res_u(s, jj + s->jp0);
+        const size_t P = r ? (size_t)s->ngx2 * s->ngz2 : PL;
+        plane_to_phys_r(s, r, s->p + 2 * (size_t)jj * nc, A, scr);
+        for (size_t n = 0; n < P; ++n) { acc[6] += A[n]; acc[7] += A[n] * A[n]; }
       }
       for (int r = 0; r < 13; ++r) s->stat[(size_t)r * L + jj] += acc[r];
     }

@@ -42,6 +42,14 @@
  * i = 0..N1/2 (kx = alp*i), kk = 0..N2-1 in FFT order (kz = bet*kk for
  * kk < N2/2, bet*(kk-N2) otherwise); j runs over the field's own y range.
  * A physical plane is [k][i] real with k = 0..Ngalz-1, i = 0..Ngalx-1.
+ *
+ * Bands.  With two resolutions every level still holds the wall bands' (fine)
+ * mode set.  Modes of the middle band's set are the long columns and live on
+ * every level; the other modes are the short columns, which live only in the
+ * wall bands (u: N(4,0)..N(4,1)+1 and N(4,2)..N(4,3)+1, v: N(3,0)..N(3,1)+1
+ * and N(3,2)..N(3,3)+1, p: N(4,0)+1..N(4,1) and N(4,2)+1..N(4,3)) and are
+ * zero elsewhere; the physical planes of the middle band (u: N(4,1)+1..N(4,2),
+ * v: N(3,1)+1..N(3,2)) are transformed at the middle band's resolution.
  */
 #ifndef LH_ORACLE_H
 #define LH_ORACLE_H
@@ -84,6 +92,10 @@ typedef struct lho_config {
   int32_t dsty, dstx, dstz, ntilex, ntilez;
   int32_t flag_ctpress;     /* 0 constant flow rate, 1 constant pressure gradient */
   int32_t nthreads;         /* OpenMP threads, <=0: library default */
+  /* Variable-resolution bands (start.f90:95-118, 1037-1145): physical points of
+   * the middle band; 0 or equal to ngalx/ngalz = one resolution everywhere.
+   * ngalx/ngalz are then the wall bands' (Ngal(1:2,1) = Ngal(1:2,3)). */
+  int32_t ngalx2, ngalz2;
 } lho_config;
 
 /* Sizes exposed to callers (all indices are the reference's global y indices). */

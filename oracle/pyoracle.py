@@ -48,7 +48,7 @@ class Config(C.Structure):
         ("dyq", C.c_double), ("ppp", C.c_int32), ("geometry_type", C.c_int32),
         ("posth", C.c_double), ("dsty", C.c_int32), ("dstx", C.c_int32), ("dstz", C.c_int32),
         ("ntilex", C.c_int32), ("ntilez", C.c_int32), ("flag_ctpress", C.c_int32),
-        ("nthreads", C.c_int32),
+        ("nthreads", C.c_int32), ("ngalx2", C.c_int32), ("ngalz2", C.c_int32),
     ]
 
 
@@ -150,9 +150,10 @@ class Oracle:
     """One oracle solver instance (FP64, CPU)."""
 
     def __init__(self, Re, alp, bet, ngalx, ngalz, ny, dyq=13.6, ppp=5, geometry_type=3, posth=0.2,
-                 dsty=16, dstx=2, dstz=4, ntilex=12, ntilez=6, flag_ctpress=0, nthreads=0):
+                 dsty=16, dstx=2, dstz=4, ntilex=12, ntilez=6, flag_ctpress=0, nthreads=0, ngalx2=0, ngalz2=0):
+        """ngalx2/ngalz2: the middle band's physical points (0: one resolution everywhere)."""
         cfg = Config(Re, alp, bet, ngalx, ngalz, ny, dyq, ppp, geometry_type, posth, dsty, dstx, dstz,
-                     ntilex, ntilez, flag_ctpress, nthreads)
+                     ntilex, ntilez, flag_ctpress, nthreads, ngalx2, ngalz2)
         err = C.create_string_buffer(256)
         h = lib().lho_create(C.byref(cfg), err, 256)
         if not h:
