@@ -157,20 +157,25 @@ def read_input(path: str) -> Input:
 
 
 class Config:
-    """The input.in quantities the time step depends on (single x/z resolution)."""
+    """The input.in quantities the time step depends on.  ngalx/ngalz are the
+    wall bands' physical points (Ngalx1, Ngalz1); ngalx2/ngalz2 the middle
+    band's (Ngalx2, Ngalz2; 0 = the same, one resolution everywhere)."""
 
     def __init__(self, Re=2800.0, alp=1.0, bet=2.0, ngalx=96, ngalz=96, ny=97, dyq=13.6, ppp=5,
                  geometry_type=3, posth=0.2, dsty=16, dstx=2, dstz=4, ntilex=12, ntilez=6, flag_ctpress=0,
-                 mpgx=0.0, CFL=0.5):
+                 mpgx=0.0, CFL=0.5, ngalx2=0, ngalz2=0):
         self.__dict__.update(dict(Re=Re, alp=alp, bet=bet, ngalx=ngalx, ngalz=ngalz, ny=ny, dyq=dyq, ppp=ppp,
                                   geometry_type=geometry_type, posth=posth, dsty=dsty, dstx=dstx, dstz=dstz,
-                                  ntilex=ntilex, ntilez=ntilez, flag_ctpress=flag_ctpress, mpgx=mpgx, CFL=CFL))
+                                  ntilex=ntilex, ntilez=ntilez, flag_ctpress=flag_ctpress, mpgx=mpgx, CFL=CFL,
+                                  ngalx2=ngalx2, ngalz2=ngalz2))
 
     def to_input(self) -> Input:
         i = Input()
         i.Re, i.alp, i.bet = self.Re, self.alp, self.bet
-        i.ngalx1 = i.ngalx2 = self.ngalx
-        i.ngalz1 = i.ngalz2 = self.ngalz
+        i.ngalx1 = self.ngalx
+        i.ngalx2 = self.ngalx2 or self.ngalx
+        i.ngalz1 = self.ngalz
+        i.ngalz2 = self.ngalz2 or self.ngalz
         i.ny, i.dyq, i.ppp = self.ny, self.dyq, self.ppp
         i.geometry_type, i.posth = self.geometry_type, self.posth
         i.dsty, i.dstx, i.dstz, i.ntilex, i.ntilez = self.dsty, self.dstx, self.dstz, self.ntilex, self.ntilez
@@ -180,12 +185,11 @@ class Config:
 
     @staticmethod
     def from_input(i: Input) -> "Config":
-        if i.ngalx1 != i.ngalx2 or i.ngalz1 != i.ngalz2:
-            raise LhError("bands with different x/z resolutions are not built")
         return Config(Re=i.Re, alp=i.alp, bet=i.bet, ngalx=i.ngalx1, ngalz=i.ngalz1, ny=i.ny, dyq=i.dyq,
                       ppp=i.ppp, geometry_type=i.geometry_type, posth=i.posth, dsty=i.dsty, dstx=i.dstx,
                       dstz=i.dstz, ntilex=i.ntilex, ntilez=i.ntilez, flag_ctpress=i.flag_ctpress, mpgx=i.mpgx,
-                      CFL=i.CFL)
+                      CFL=i.CFL, ngalx2=i.ngalx2 if i.ngalx2 != i.ngalx1 else 0,
+                      ngalz2=i.ngalz2 if i.ngalz2 != i.ngalz1 else 0)
 
 
 def setup(inp: Input):

@@ -76,6 +76,9 @@ struct lh_handle {
   DevScalars* sc = nullptr;
   PlanStore pz, ph, pf;  // z (Ngalz), x half length (Ngalx/2), x full length (Ngalx)
   double2* rtw = nullptr;
+  PlanStore pz2, ph2, pf2;  // the same for the middle band (bands only)
+  double2* rtw2 = nullptr;
+  Dims dmid{};              // the middle band's plane geometry (bands only)
   int tx = 8, chunk = 16;
   // state
   double t_now = 0, dt = 0;
@@ -199,17 +202,42 @@ size_t field_elems(const lh_handle* h, char grid) {
   return (size_t)ny * h->d.np;
 }
 
-// Helmholtz LU for the three substages (LU_build + LU_dec, tridLU_3D_IB.f90:
-// 427-493,601-640) and the unit-gradient response of mode (0,0) (LUsol0,
-// :398-424) for the current dt.
+// LU_build + LU_dec (tridLU_3D_IB.f90:427-493,601-640) over levels lo..hi of
+// one grid (coefficients c = dyu2i or dyv2i per level), boundary rows
+// [1, gwl] and [gwh, 1] (u) or identity rows (v: gwl = gwh = 0).
+void helm_lu_host(double* a1, double* a2, double* a3, const std::vector<double>& c, int lo, int hi, double beta,
+                  double gwl, double gwh) {
+  a1[lo] = 0.0; a2[lo] = 1.0; a3[lo] = gwl;
+  for (int j = lo + 1; j < hi; ++j) {
+    a1[j] = -beta * c[3 * j];
+    a2[j] = 1.0 - beta * (c[3 * j + 1]);
+    a3[j] = -beta * c[3 * j + 2];
+  }
+  a1[hi] = gwh; a2[hi] = 1.0; a3[hi] = 0.0;
+  a2[lo] = 1.0 / a2[lo];
+  for (int j = lo + 1; j <= hi; ++j) {
+    a3[j - 1] = a3[j - 1] * a2[j - 1];
+    a2[j] = 1.0 / (a2[j] - a1[j] * a3[j - 1]);
+  }
+}
+
+// Helmholtz LU for the three substages (long columns over the whole channel
+// with band 2's gridweighting; with bands also the short columns' bottom and
+// top bands with bands 1 and 3's) and the unit-gradient response of mode
+// (0,0) (LUsol0, :398-424) for the current dt.
 int build_dt_tables(lh_handle* h) {
   const Dims& d = h->d;
   const int nyu = d.nyu, nyv = d.nyv, n0 = d.nn + 3;
   const size_t np = d.np;
-  std::vector<double> all(3 * 3 * nyu + 3 * 3 * nyv + 3 * n0 + 3 * np);
+  const int nb = d.banded ? 3 : 1;  // LU sets per grid: long (, bottom, top)
+  std::vector<double> all(nb * 9 * (size_t)nyu + nb * 9 * (size_t)nyv + 3 * n0 + 3 * np);
   double* luu = all.data();
   double* luv = luu + 9 * nyu;
-  double* u11 = luv + 9 * nyv;
+  double* luu1 = luv + 9 * nyv;       // used with bands only
+  double* luu3 = luu1 + 9 * nyu;
+  double* luv1 = luu3 + 9 * nyu;
+  double* luv3 = luv1 + 9 * nyv;
+  double* u11 = all.data() + nb * 9 * (size_t)nyu + nb * 9 * (size_t)nyv;
   double* iaxz = u11 + 3 * n0;
   for (int k = 0; k < 3; ++k) {
     const double beta = h->bRK[k] * h->dt / h->Re;
@@ -217,19 +245,16 @@ int build_dt_tables(lh_handle* h) {
       const int ny = grid == 0 ? nyu : nyv;
       const std::vector<double>& c = grid == 0 ? h->dyu2i : h->dyv2i;
       double* a1 = (grid == 0 ? luu : luv) + (size_t)k * 3 * ny;
-      double* a2 = a1 + ny;
-      double* a3 = a2 + ny;
-      a1[0] = 0.0; a2[0] = 1.0; a3[0] = grid == 0 ? h->gw[1][0] : 0.0;
-      for (int j = 1; j < ny - 1; ++j) {
-        a1[j] = -beta * c[3 * j];
-        a2[j] = 1.0 - beta * (c[3 * j + 1]);
-        a3[j] = -beta * c[3 * j + 2];
-      }
-      a1[ny - 1] = grid == 0 ? h->gw[1][1] : 0.0; a2[ny - 1] = 1.0; a3[ny - 1] = 0.0;
-      a2[0] = 1.0 / a2[0];
-      for (int j = 1; j < ny; ++j) {
-        a3[j - 1] = a3[j - 1] * a2[j - 1];
-        a2[j] = 1.0 / (a2[j] - a1[j] * a3[j - 1]);
+      helm_lu_host(a1, a1 + ny, a1 + 2 * ny, c, 0, ny - 1, beta, grid == 0 ? h->gw[1][0] : 0.0,
+                   grid == 0 ? h->gw[1][1] : 0.0);
+      if (d.banded) {
+        const int e1 = grid == 0 ? d.Nu1 + 1 : d.Nv1 + 1, s3 = grid == 0 ? d.Nu2 : d.Nv2;
+        double* b1 = (grid == 0 ? luu1 : luv1) + (size_t)k * 3 * ny;
+        double* b3 = (grid == 0 ? luu3 : luv3) + (size_t)k * 3 * ny;
+        helm_lu_host(b1, b1 + ny, b1 + 2 * ny, c, 0, e1, beta, grid == 0 ? h->gw[0][0] : 0.0,
+                     grid == 0 ? h->gw[0][1] : 0.0);
+        helm_lu_host(b3, b3 + ny, b3 + 2 * ny, c, s3, ny - 1, beta, grid == 0 ? h->gw[2][0] : 0.0,
+                     grid == 0 ? h->gw[2][1] : 0.0);
       }
     }
     // LU_build0 on global indices 0..nn+2
@@ -273,10 +298,39 @@ int build_dt_tables(lh_handle* h) {
   CU(h, cudaMemcpyAsync(h->tabs, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
   h->t.lu_u = h->tabs;
   h->t.lu_v = h->tabs + 9 * nyu;
-  h->t.u11 = h->tabs + 9 * nyu + 9 * nyv;
-  h->t.iaxz = h->tabs + 9 * nyu + 9 * nyv + 3 * n0;
+  h->t.lu_u1 = d.banded ? h->tabs + 9 * nyu + 9 * nyv : h->t.lu_u;
+  h->t.lu_u3 = d.banded ? h->t.lu_u1 + 9 * nyu : h->t.lu_u;
+  h->t.lu_v1 = d.banded ? h->t.lu_u3 + 9 * nyu : h->t.lu_v;
+  h->t.lu_v3 = d.banded ? h->t.lu_v1 + 9 * nyv : h->t.lu_v;
+  h->t.u11 = h->tabs + nb * 9 * (size_t)nyu + nb * 9 * (size_t)nyv;
+  h->t.iaxz = h->t.u11 + 3 * n0;
   CU(h, cudaStreamSynchronize(h->st));
   return LH_OK;
+}
+
+// The plane work of the nonlinear term per band: which geometry and transforms
+// a band's planes use, and the centre and face levels it forms products on
+// (planelim, start.f90:1326-1378).
+struct BandLaunch {
+  const Dims* d;
+  const FftPlan *pz, *ph, *pf;
+  const double2* rtw;
+  int c_lo, c_hi, f_lo, f_hi;
+};
+int band_launches(const lh_handle* h, BandLaunch* out) {
+  const Dims& d = h->d;
+  const BandLaunch fine{&d, &h->pz.plan, &h->ph.plan, &h->pf.plan, h->rtw, 0, 0, 0, 0};
+  if (!d.banded) {
+    out[0] = fine;
+    out[0].c_lo = 1; out[0].c_hi = d.nyu - 2; out[0].f_lo = 1; out[0].f_hi = d.nyv - 2;
+    return 1;
+  }
+  out[0] = fine;
+  out[0].c_lo = 1; out[0].c_hi = d.Nu1; out[0].f_lo = 1; out[0].f_hi = d.Nv1;
+  out[1] = BandLaunch{&h->dmid, &h->pz2.plan, &h->ph2.plan, &h->pf2.plan, h->rtw2, d.Nu1 + 1, d.Nu2, d.Nv1 + 1, d.Nv2};
+  out[2] = fine;
+  out[2].c_lo = d.Nu2 + 1; out[2].c_hi = d.nyu - 2; out[2].f_lo = d.Nv2 + 1; out[2].f_hi = d.nyv - 2;
+  return 3;
 }
 
 template <typename R>
@@ -285,40 +339,51 @@ int enqueue_substage(lh_handle* h, int k, int upto) {
   const Dims& d = h->d;
   cudaStream_t st = h->st;
   const double beta = h->bRK[k] * h->dt / h->Re;
-  // nonlinear: z-inverse of u, w (interior centres) and v (interior faces)
-  {
-    ZJobs<R> J{};
-    J.j[0] = ZJob<R>{h->u1, nullptr, (T2*)h->mixu + d.mp, nullptr, 1, d.nyu - 2};
-    J.j[1] = ZJob<R>{h->u3, nullptr, (T2*)h->mixw + d.mp, nullptr, 1, d.nyu - 2};
-    J.j[2] = ZJob<R>{h->u2, nullptr, (T2*)h->mixv + d.mp, nullptr, 1, d.nyv - 2};
-    J.njobs = 3;
-    J.maxlev = d.nyu - 2;
-    launch_zinv<R>(J, d, h->pz.plan, h->tx, st);
-    mark(h, K_ZINV);
-  }
-  {
-    ProdArgs<R> a{};
-    a.mu = (const T2*)h->mixu;
-    a.mw = (const T2*)h->mixw;
-    a.mv = (const T2*)h->mixv;
-    for (int i = 0; i < 6; ++i) a.out[i] = (T2*)h->mixp[i];
-    a.wc = h->t.wc; a.wf = h->t.wf; a.dyc = h->t.dyc;
-    a.dxi = d.ngx / h->Lx; a.dzi = d.ngz / h->Lz;
-    a.sc = h->sc; a.want_cfl = 0; a.chunk = h->chunk;
-    launch_xprod<R>(a, d, h->ph.plan, h->pf.plan, h->rtw, st);
-    mark(h, K_XPROD);
-  }
-  {
-    ZJobs<R> J{};
-    double2* outs[6] = {h->puu, h->puw, h->pww, h->pvv, h->puv, h->pvw};
-    for (int i = 0; i < 6; ++i) {
-      const int nl = i < 4 ? d.nyu - 2 : d.nyv - 2;
-      J.j[i] = ZJob<R>{nullptr, outs[i], (T2*)h->mixp[i] + d.mp, nullptr, 1, nl};
+  // nonlinear, one band at a time (one band without variable resolution): z-inverse of the levels the
+  // band's products need, products, z-forward of the band's product planes
+  BandLaunch bl[3];
+  const int nbl = band_launches(h, bl);
+  for (int b = 0; b < nbl; ++b) {
+    const BandLaunch& B = bl[b];
+    const Dims& db = *B.d;
+    const int L0 = std::min(B.c_lo, B.f_lo + 1), L1 = std::max(B.c_hi, B.f_hi + 1);
+    {
+      const int ul = std::max(1, L0 - 1), uh = std::min(d.nyu - 2, L1);
+      const int vl = std::max(1, L0 - 1), vh = std::min(d.nyv - 2, L1);
+      ZJobs<R> J{};
+      J.j[0] = ZJob<R>{h->u1, nullptr, (T2*)h->mixu + (size_t)ul * db.mp, nullptr, ul, uh - ul + 1};
+      J.j[1] = ZJob<R>{h->u3, nullptr, (T2*)h->mixw + (size_t)ul * db.mp, nullptr, ul, uh - ul + 1};
+      J.j[2] = ZJob<R>{h->u2, nullptr, (T2*)h->mixv + (size_t)vl * db.mp, nullptr, vl, std::max(0, vh - vl + 1)};
+      J.njobs = 3;
+      J.maxlev = uh - ul + 1;
+      launch_zinv<R>(J, db, *B.pz, h->tx, st);
+      mark(h, K_ZINV);
     }
-    J.njobs = 6;
-    J.maxlev = d.nyu - 2;
-    launch_zfwd<R>(J, d, h->pz.plan, h->tx, 1.0 / d.ngz, st);
-    mark(h, K_ZFWD);
+    {
+      ProdArgs<R> a{};
+      a.mu = (const T2*)h->mixu;
+      a.mw = (const T2*)h->mixw;
+      a.mv = (const T2*)h->mixv;
+      for (int i = 0; i < 6; ++i) a.out[i] = (T2*)h->mixp[i];
+      a.wc = h->t.wc; a.wf = h->t.wf; a.dyc = h->t.dyc;
+      a.dxi = db.ngx / h->Lx; a.dzi = db.ngz / h->Lz;
+      a.sc = h->sc; a.want_cfl = 0; a.chunk = h->chunk;
+      a.c_lo = B.c_lo; a.c_hi = B.c_hi; a.f_lo = B.f_lo; a.f_hi = B.f_hi;
+      launch_xprod<R>(a, db, *B.ph, *B.pf, B.rtw, st);
+      mark(h, K_XPROD);
+    }
+    {
+      ZJobs<R> J{};
+      double2* outs[6] = {h->puu, h->puw, h->pww, h->pvv, h->puv, h->pvw};
+      for (int i = 0; i < 6; ++i) {
+        const int lo = i < 4 ? B.c_lo : B.f_lo, hi = i < 4 ? B.c_hi : B.f_hi;
+        J.j[i] = ZJob<R>{nullptr, outs[i], (T2*)h->mixp[i] + (size_t)lo * db.mp, nullptr, lo, std::max(0, hi - lo + 1)};
+      }
+      J.njobs = 6;
+      J.maxlev = std::max(B.c_hi - B.c_lo + 1, B.f_hi - B.f_lo + 1);
+      launch_zfwd<R>(J, db, *B.pz, h->tx, 1.0 / db.ngz, st);
+      mark(h, K_ZFWD);
+    }
   }
   {
     AsmArgs a{};
@@ -478,8 +543,6 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
   if (prm->abi_version != LH_ABI_VERSION) return fail(nullptr, LH_EINVAL, "abi_version %d != %d", prm->abi_version, LH_ABI_VERSION);
   auto Nf = [&](int row, int band) { return prm->N[band * 4 + row - 1]; };
   auto Gf = [&](int row, int band) { return prm->Ngal[band * 4 + row - 1]; };
-  if (Gf(1, 1) != Gf(1, 2) || Gf(2, 1) != Gf(2, 2))
-    return fail(nullptr, LH_EUNSUPPORTED, "bands with different x/z resolutions (short columns) are not built");
   if (prm->precision != LH_PREC_FP64 && prm->precision != LH_PREC_MIXED) return fail(nullptr, LH_EINVAL, "bad precision");
   if (prm->geometry_type != 0 && prm->geometry_type != 3) return fail(nullptr, LH_EUNSUPPORTED, "geometry_type %d has no forcing builder", prm->geometry_type);
   lh_handle* h = new lh_handle();
@@ -510,7 +573,22 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
   d.nz = nz;
   d.np = d.nkx * d.nz;
   d.mp = d.nkx * d.ngz;
+  d.spitch = d.nkx;
+  d.snz = d.nz;
   d.ju0 = Nf(4, 0);
+  // variable-resolution bands (start.f90:95-118): the middle band's resolution
+  d.ngx2 = Gf(1, 2); d.ngz2 = Gf(2, 2);
+  d.banded = (d.ngx2 != d.ngx || d.ngz2 != d.ngz);
+  {
+    const int nx2 = Nf(1, 2), nz2 = Nf(2, 2);
+    if (nx2 != 2 * (d.ngx2 / 3) || nz2 != 2 * (d.ngz2 / 3) || d.ngx2 < 6 || d.ngz2 < 6 || (d.ngx2 & 1) || (nz2 & 1) ||
+        d.ngx2 > d.ngx || d.ngz2 > d.ngz || Gf(1, 3) != d.ngx || Gf(2, 3) != d.ngz)
+      return bail(fail(h, LH_EINVAL, "inconsistent band resolutions (the middle band may not be finer than the walls')"));
+    d.nkx2 = nx2 / 2 + 1;
+    d.nz2 = nz2;
+  }
+  d.Nu1 = Nf(4, 1) - d.ju0; d.Nu2 = Nf(4, 2) - d.ju0;
+  d.Nv1 = Nf(3, 1) - d.ju0; d.Nv2 = Nf(3, 2) - d.ju0;
   if (Nf(3, 0) != d.ju0) return bail(fail(h, LH_EINVAL, "N(3,0) != N(4,0)"));
   d.nyu = Nf(4, 3) + 1 - Nf(4, 0) + 1;
   d.nyv = Nf(3, 3) + 1 - Nf(3, 0) + 1;
@@ -518,6 +596,8 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
   d.nn = prm->nn;
   if (d.nyv != d.nyu - 1 || d.nyp != d.nyu - 2 || d.nyu < 6) return bail(fail(h, LH_EINVAL, "inconsistent y grid sizes"));
   if (d.nn + 2 - d.ju0 >= d.nyu || d.ju0 > 0) return bail(fail(h, LH_EINVAL, "nn outside the u grid"));
+  if (d.banded && !(d.Nu1 >= 2 && d.Nv1 == d.Nu1 - 1 && d.Nu2 > d.Nu1 + 1 && d.Nv2 == d.Nu2 && d.Nu2 < d.nyu - 3))
+    return bail(fail(h, LH_EINVAL, "band limits N(3:4,1:2) do not describe three bands"));
   h->Re = prm->Re; h->alp = prm->alp; h->bet = prm->bet;
   if (!(h->Re > 0) || !(h->alp > 0) || !(h->bet > 0)) return bail(fail(h, LH_EINVAL, "Re, alp, bet must be positive"));
   h->Lx = 2.0 * (double)kPi / h->alp;
@@ -551,6 +631,22 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
   if ((rc = build_plan(h, h->pz, d.ngz, d.nz / 2)) || (rc = build_plan(h, h->ph, d.ngx / 2, 0)) ||
       (rc = build_plan(h, h->pf, d.ngx, 0)))
     return bail(rc);
+  if (d.banded) {
+    // the middle band's planes: their own transform lengths and mode counts, the same storage
+    Dims& c = h->dmid;
+    c = d;
+    c.ngx = d.ngx2; c.ngz = d.ngz2; c.nkx = d.nkx2; c.nz = d.nz2;
+    c.mp = c.nkx * c.ngz;
+    if ((rc = build_plan(h, h->pz2, c.ngz, c.nz / 2)) || (rc = build_plan(h, h->ph2, c.ngx / 2, 0)) ||
+        (rc = build_plan(h, h->pf2, c.ngx, 0)))
+      return bail(rc);
+    std::vector<double2> rt(c.ngx / 2 + 1);
+    for (int k = 0; k <= c.ngx / 2; ++k) {
+      const long double a = 2.0L * kPi * (long double)k / (long double)c.ngx;
+      rt[k] = double2{(double)cosl(a), -(double)sinl(a)};
+    }
+    if ((rc = upload(h, &h->rtw2, rt))) return bail(rc);
+  }
   {
     std::vector<double2> rt(d.ngx / 2 + 1);
     for (int k = 0; k <= d.ngx / 2; ++k) {
@@ -624,6 +720,10 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
     }
     h->nibu = (int)levu.size();
     h->nibv = (int)levv.size();
+    for (int l : levu)
+      if (coarse_u(d, l)) return bail(fail(h, LH_EUNSUPPORTED, "canopy planes must lie in the wall bands"));
+    for (int l : levv)
+      if (coarse_v(d, l)) return bail(fail(h, LH_EUNSUPPORTED, "canopy planes must lie in the wall bands"));
     const size_t pl = (size_t)d.ngx * d.ngz;
     std::vector<uint8_t> mu(pl * std::max(h->nibu, 1), 0), mv(pl * std::max(h->nibv, 1), 0);
     auto mark = [&](const int32_t* L, int n, const std::vector<int>& lev, std::vector<uint8_t>& m) -> int {
@@ -1070,20 +1170,28 @@ int lh_cfl_dt(lh_handle* h, double cfl, double* dt_out) {
   auto run = [&](auto tag) {
     using R = decltype(tag);
     using T2 = cpx_t<R>;
-    ZJobs<R> J{};
-    J.j[0] = ZJob<R>{h->u1, nullptr, (T2*)h->mixu + d.mp, nullptr, 1, d.nyu - 2};
-    J.j[1] = ZJob<R>{h->u3, nullptr, (T2*)h->mixw + d.mp, nullptr, 1, d.nyu - 2};
-    J.j[2] = ZJob<R>{h->u2, nullptr, (T2*)h->mixv + d.mp, nullptr, 1, d.nyv - 2};
-    J.njobs = 3;
-    J.maxlev = d.nyu - 2;
-    launch_zinv<R>(J, d, h->pz.plan, h->tx, h->st);
-    ProdArgs<R> a{};
-    a.mu = (const T2*)h->mixu; a.mw = (const T2*)h->mixw; a.mv = (const T2*)h->mixv;
-    for (int i = 0; i < 6; ++i) a.out[i] = (T2*)h->mixp[i];
-    a.wc = h->t.wc; a.wf = h->t.wf; a.dyc = h->t.dyc;
-    a.dxi = d.ngx / h->Lx; a.dzi = d.ngz / h->Lz;
-    a.sc = h->sc; a.want_cfl = 1; a.chunk = h->chunk;
-    launch_xprod<R>(a, d, h->ph.plan, h->pf.plan, h->rtw, h->st);
+    BandLaunch bl[3];
+    const int nbl = band_launches(h, bl);
+    for (int b = 0; b < nbl; ++b) {  // each centre plane at its band's resolution
+      const BandLaunch& B = bl[b];
+      const Dims& db = *B.d;
+      const int ul = std::max(1, B.c_lo - 1), uh = B.c_hi, vl = ul, vh = std::min(d.nyv - 2, B.c_hi);
+      ZJobs<R> J{};
+      J.j[0] = ZJob<R>{h->u1, nullptr, (T2*)h->mixu + (size_t)ul * db.mp, nullptr, ul, uh - ul + 1};
+      J.j[1] = ZJob<R>{h->u3, nullptr, (T2*)h->mixw + (size_t)ul * db.mp, nullptr, ul, uh - ul + 1};
+      J.j[2] = ZJob<R>{h->u2, nullptr, (T2*)h->mixv + (size_t)vl * db.mp, nullptr, vl, vh - vl + 1};
+      J.njobs = 3;
+      J.maxlev = uh - ul + 1;
+      launch_zinv<R>(J, db, *B.pz, h->tx, h->st);
+      ProdArgs<R> a{};
+      a.mu = (const T2*)h->mixu; a.mw = (const T2*)h->mixw; a.mv = (const T2*)h->mixv;
+      for (int i = 0; i < 6; ++i) a.out[i] = (T2*)h->mixp[i];
+      a.wc = h->t.wc; a.wf = h->t.wf; a.dyc = h->t.dyc;
+      a.dxi = db.ngx / h->Lx; a.dzi = db.ngz / h->Lz;
+      a.sc = h->sc; a.want_cfl = 1; a.chunk = h->chunk;
+      a.c_lo = B.c_lo; a.c_hi = B.c_hi; a.f_lo = B.c_lo; a.f_hi = B.c_lo - 1;  // centres only
+      launch_xprod<R>(a, db, *B.ph, *B.pf, B.rtw, h->st);
+    }
   };
   if (h->precision == LH_PREC_MIXED) run(0.0f);
   else run(0.0);

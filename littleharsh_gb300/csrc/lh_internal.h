@@ -8,16 +8,54 @@
 
 namespace lh {
 
-// Geometry of the single band of long columns (every (kx,kz) column spans the
-// whole channel, as when Ngalx1 == Ngalx2 and Ngalz1 == Ngalz2).
+// Grid sizes.  Every level stores the wall bands' mode set (nkx x nz, the only
+// one without variable-resolution bands).  With bands (Ngalx1 != Ngalx2,
+// start.f90:95-118,1037-1145) the modes of the middle band's set are the long
+// columns and span all levels; the others are short columns that live only in
+// the wall bands (u levels 0..Nu1+1 and Nu2..nyu-1, v levels 0..Nv1+1 and
+// Nv2..nyv-1, p levels 0..Nu1-1 and Nu2..nyp-1, end rows included) and are
+// zero elsewhere.  A Dims passed to the plane kernels of the middle band has
+// that band's nkx/nz/ngx/ngz/mp, and spitch/snz still describe the storage.
 struct Dims {
-  int nkx, nz, ngx, ngz;   // N1/2+1, N2, Ngal1, Ngal2
-  int np;                  // spectral plane: nkx*nz complex
+  int nkx, nz, ngx, ngz;   // N1/2+1, N2, Ngal1, Ngal2 of the resolution the kernel works at
+  int np;                  // stored spectral plane: spitch*snz complex
   int mp;                  // mixed plane (after the z transform): nkx*ngz complex
   int nyu, nyv, nyp;       // levels of the u, v and p grids
   int nn;                  // reference nn (= ny-2); u11 spans 0..nn+2
   int ju0;                 // global index of u level 0 (= jv0 = N(4,0)); p level 0 is ju0+1
+  int spitch, snz;         // stored mode set: kx count (row pitch) and kz count
+  int banded;              // 1: two resolutions (short and long columns)
+  int nkx2, nz2;           // the middle band's mode set (long columns)
+  int ngx2, ngz2;          // the middle band's physical points
+  int Nu1, Nu2, Nv1, Nv2;  // level indices of N(4,1), N(4,2), N(3,1), N(3,2): the middle band's planes are
+                           // u levels Nu1+1..Nu2 and v levels Nv1+1..Nv2
 };
+
+// Long column test for stored mode (i, kk) (columns_long_list, start.f90:1100-1117).
+__host__ __device__ inline bool is_long(const Dims& d, int i, int kk) {
+  if (!d.banded) return true;
+  const int kz = kk < d.snz / 2 ? kk : kk - d.snz;
+  return i < d.nkx2 && kz >= -(d.nz2 / 2) && kz < d.nz2 / 2;
+}
+// Where a column's y range (jlim, start.f90:1147-1175) puts level jj: 0 outside,
+// 1 interior, 2 end row.
+__host__ __device__ inline int lev_u(const Dims& d, bool lng, int jj) {
+  if (lng) return (jj == 0 || jj == d.nyu - 1) ? 2 : 1;
+  if (jj == 0 || jj == d.Nu1 + 1 || jj == d.Nu2 || jj == d.nyu - 1) return 2;
+  return ((jj > 0 && jj <= d.Nu1) || (jj > d.Nu2 && jj < d.nyu - 1)) ? 1 : 0;
+}
+__host__ __device__ inline int lev_v(const Dims& d, bool lng, int jj) {
+  if (lng) return (jj == 0 || jj == d.nyv - 1) ? 2 : 1;
+  if (jj == 0 || jj == d.Nv1 + 1 || jj == d.Nv2 || jj == d.nyv - 1) return 2;
+  return ((jj > 0 && jj <= d.Nv1) || (jj > d.Nv2 && jj < d.nyv - 1)) ? 1 : 0;
+}
+// p level jp (global j = ju0 + 1 + jp) inside the column
+__host__ __device__ inline bool lev_p(const Dims& d, bool lng, int jp) {
+  return lng || jp < d.Nu1 || jp >= d.Nu2;
+}
+// the middle band's planes
+__host__ __device__ inline bool coarse_u(const Dims& d, int jj) { return d.banded && jj > d.Nu1 && jj <= d.Nu2; }
+__host__ __device__ inline bool coarse_v(const Dims& d, int jj) { return d.banded && jj > d.Nv1 && jj <= d.Nv2; }
 
 // Read-only per-run tables in device memory.
 struct Tables {
@@ -33,8 +71,12 @@ struct Tables {
   const double* wf;    // [nyv] weight of centre j+1 in the face-j interpolation of u, w
   const double* dyc;   // [nyu] 1/(yv(j)-yv(j-1)) at centres, for the CFL number
   const double* dyvw;  // [nn+2] yv(j)-yv(j-1), j = 1..nn+1 at index j (flow rate)
-  const double* lu_u;  // [3 kRK][3][nyu] Helmholtz LU (a1, 1/diag, scaled a3), u grid
+  const double* lu_u;  // [3 kRK][3][nyu] Helmholtz LU (a1, 1/diag, scaled a3), u grid, long columns
   const double* lu_v;  // [3 kRK][3][nyv] same, v grid
+  const double* lu_u1; // [3 kRK][3][nyu] short columns' bottom band (levels 0..Nu1+1; with bands only)
+  const double* lu_u3; // [3 kRK][3][nyu] short columns' top band (levels Nu2..nyu-1)
+  const double* lu_v1; // [3 kRK][3][nyv] (levels 0..Nv1+1)
+  const double* lu_v3; // [3 kRK][3][nyv] (levels Nv2..nyv-1)
   const double* u11;   // [3 kRK][nn+3] unit-gradient response of mode (0,0)
   const double* iaxz;  // [3 kRK][np] 1/axz = 1/(1 - beta_k (k2x + k2z)) per column
   const double* dg1;   // [nyp] pressure LU lower diagonal (column independent)
@@ -96,6 +138,8 @@ struct ProdArgs {
   DevScalars* sc;       // CFL maximum accumulated here when want_cfl
   int want_cfl;
   int chunk;
+  // levels this launch forms products on (a band's planes): centres c_lo..c_hi, faces f_lo..f_hi
+  int c_lo, c_hi, f_lo, f_hi;
 };
 template <typename R>
 void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const FftPlan& pf, const double2* rtw,

@@ -95,6 +95,13 @@ int sizes(lh_handle* h, Sz* s) {
   return LH_OK;
 }
 
+// The files of a run with variable-resolution bands keep the middle band's
+// planes at its own mode set (per-plane nx, nz records); that layout is not
+// written here.
+bool banded(const lh_params* prm) {
+  return prm->Ngal[1 * 4 + 0] != prm->Ngal[2 * 4 + 0] || prm->Ngal[1 * 4 + 1] != prm->Ngal[2 * 4 + 1];
+}
+
 }  // namespace
 
 extern "C" {
@@ -103,6 +110,7 @@ int lh_write_restart(lh_handle* h, const lh_params* prm, const double* yu, const
                      const char* name, int32_t iter) {
   if (!h || !prm || !dir || !name || !yu || !yv) return LH_EINVAL;
   g_cur = h;
+  if (banded(prm)) return io_fail(LH_EUNSUPPORTED, "files of runs with variable-resolution bands are not written");
   Sz s;
   int rc = sizes(h, &s);
   if (rc) return rc;
@@ -188,6 +196,7 @@ int lh_write_stats(lh_handle* h, const lh_params* prm, const double* yu, const d
                    const double* dthdyv, const char* path, int32_t iter) {
   if (!h || !prm || !yu || !yv || !dthdyu || !dthdyv || !path) return LH_EINVAL;
   g_cur = h;
+  if (banded(prm)) return io_fail(LH_EUNSUPPORTED, "files of runs with variable-resolution bands are not written");
   Sz s;
   int rc = sizes(h, &s);
   if (rc) return rc;
@@ -243,6 +252,7 @@ int lh_write_spectra(lh_handle* h, const lh_params* prm, const double* yu, const
                      const double* dthdyv, const char* dir, const char* name, int32_t iter) {
   if (!h || !prm || !yu || !yv || !dthdyu || !dthdyv || !dir || !name) return LH_EINVAL;
   g_cur = h;
+  if (banded(prm)) return io_fail(LH_EUNSUPPORTED, "files of runs with variable-resolution bands are not written");
   Sz s;
   int rc = sizes(h, &s);
   if (rc) return rc;

@@ -23,6 +23,7 @@
 //   flowrate  meanflow_ctU/flowrate_corr on mode (0,0) (littleharsh.f90:453-485)
 //   psolve divergence, pressure LU per column, p += psi, v_corr
 //          (littleharsh.f90:557-612,826-937; tridLU_3D_IB.f90:362-396)
+#include <algorithm>
 #include <cstdio>
 
 #include "lh_internal.h"
@@ -54,7 +55,8 @@ __global__ void __launch_bounds__(256) k_zinv(ZJobs<R> jobs, Dims d, FftPlan pz,
     const int slot = kk < h ? kk : kk + gap;
     T2 v = T2{0, 0};
     if (c < nb) {
-      const double2 s = src[(size_t)kk * d.nkx + i0 + c];
+      const int ks = kk < h ? kk : kk - d.nz + d.snz;  // row of the stored mode set
+      const double2 s = src[(size_t)ks * d.spitch + i0 + c];
       v = T2{(R)s.x, (R)s.y};
     }
     sm[pz.perm[slot] * tx + c] = v;
@@ -96,7 +98,8 @@ __global__ void __launch_bounds__(256) k_zfwd(ZJobs<R> jobs, Dims d, FftPlan pz,
     if (c < nb) {
       const int slot = kk < h ? kk : kk + gap;
       const T2 v = sm[slot * tx + c];
-      dst[(size_t)kk * d.nkx + i0 + c] = double2{(double)v.x * scale, (double)v.y * scale};
+      const int ks = kk < h ? kk : kk - d.nz + d.snz;
+      dst[(size_t)ks * d.spitch + i0 + c] = double2{(double)v.x * scale, (double)v.y * scale};
     }
   }
 }
@@ -250,8 +253,10 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
   R* vc = rowsm + 5 * ngx;
   __shared__ double cflred[8];
   const int kz = blockIdx.x;
-  const int c0 = 1 + blockIdx.y * a.chunk;
-  const int c1 = min(c0 + a.chunk - 1, d.nyu - 2);
+  // step jj forms the centre-jj products (c_lo <= jj <= c_hi) and the face-(jj-1) ones (f_lo <= jj-1 <= f_hi)
+  const int L0 = min(a.c_lo, a.f_lo + 1), L1 = max(a.c_hi, a.f_hi + 1);
+  const int c0 = L0 + blockIdx.y * a.chunk;
+  const int c1 = min(c0 + a.chunk - 1, L1);
   if (c0 > c1) return;
   const size_t rowoff = (size_t)kz * d.nkx;
   double cmax = 0.0;
@@ -277,33 +282,45 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
       for (int x = threadIdx.x; x < ngx; x += blockDim.x) vc[x] = (R)0;
       __syncthreads();
     }
-    const bool fprod = jj - 1 >= 1;  // face jj-1 interior
+    const bool cprod = jj >= a.c_lo && jj <= a.c_hi;
+    const bool fprod = jj - 1 >= a.f_lo && jj - 1 <= a.f_hi;  // face jj-1 interior and in this launch
     const R wcj = (R)a.wc[jj];
     const R wfj = fprod ? (R)a.wf[jj - 1] : (R)0;
     const double dyi = a.dyc[jj];
-    // pairs: (uu, uw), (ww, vv) at centre jj; (uv, vw) at face jj-1
+    // pairs: (uu, uw), (ww, vv) at centre jj; (uv, vw) at face jj-1 (after the centre pairs, or first)
+    const int fslot = cprod ? 2 : 0;
     for (int x = threadIdx.x; x < ngx; x += blockDim.x) {
       const R u = uc[x], w = wc[x];
-      const R v = vp[x] + wcj * (vc[x] - vp[x]);
       const int px = pf.perm[x];
-      F[px] = T2{u * u, u * w};
-      F[ngx + px] = T2{w * w, v * v};
+      if (cprod) {
+        const R v = vp[x] + wcj * (vc[x] - vp[x]);
+        F[px] = T2{u * u, u * w};
+        F[ngx + px] = T2{w * w, v * v};
+        if (a.want_cfl) {
+          const double cv = fabs((double)u) * a.dxi + fabs((double)v) * dyi + fabs((double)w) * a.dzi;
+          cmax = fmax(cmax, cv);
+        }
+      }
       if (fprod) {
         const R uf = up[x] + wfj * (u - up[x]);
         const R wf = wp[x] + wfj * (w - wp[x]);
-        F[2 * ngx + px] = T2{uf * vp[x], wf * vp[x]};
-      }
-      if (a.want_cfl) {
-        const double cv = fabs((double)u) * a.dxi + fabs((double)v) * dyi + fabs((double)w) * a.dzi;
-        cmax = fmax(cmax, cv);
+        F[fslot * ngx + px] = T2{uf * vp[x], wf * vp[x]};
       }
     }
     __syncthreads();
-    {
-      T2* rows[6] = {a.out[0] + (size_t)jj * d.mp + rowoff, a.out[1] + (size_t)jj * d.mp + rowoff,
-                     a.out[2] + (size_t)jj * d.mp + rowoff, a.out[3] + (size_t)jj * d.mp + rowoff,
-                     a.out[4] + (size_t)(jj - 1) * d.mp + rowoff, a.out[5] + (size_t)(jj - 1) * d.mp + rowoff};
-      x_forward_pairs<R>(fprod ? 3 : 2, F, rows, d, pf);
+    if (cprod || fprod) {
+      T2* rows[6];
+      int npair = 0;
+      if (cprod) {
+        for (int q = 0; q < 4; ++q) rows[q] = a.out[q] + (size_t)jj * d.mp + rowoff;
+        npair = 2;
+      }
+      if (fprod) {
+        rows[2 * npair] = a.out[4] + (size_t)(jj - 1) * d.mp + rowoff;
+        rows[2 * npair + 1] = a.out[5] + (size_t)(jj - 1) * d.mp + rowoff;
+        ++npair;
+      }
+      x_forward_pairs<R>(npair, F, rows, d, pf);
     }
     // current becomes previous
     R* t;
@@ -326,9 +343,10 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
 template <typename R>
 void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const FftPlan& pf, const double2* rtw,
                   cudaStream_t st) {
-  const int ncent = d.nyu - 2;
-  if (ncent <= 0) return;
-  dim3 grid(d.ngz, (ncent + a.chunk - 1) / a.chunk);
+  const int L0 = std::min(a.c_lo, a.f_lo + 1), L1 = std::max(a.c_hi, a.f_hi + 1);
+  const int nlev = L1 - L0 + 1;
+  if (nlev <= 0) return;
+  dim3 grid(d.ngz, (nlev + a.chunk - 1) / a.chunk);
   size_t sm = sizeof(cpx_t<R>) * 3 * (size_t)d.ngx + sizeof(R) * 6 * (size_t)d.ngx;
   k_xprod<R><<<grid, 256, sm, st>>>(a, d, ph, pf, rtw);
 }
@@ -406,10 +424,16 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
   // division, which costs ~10 FP64 instructions on a part with little FP64 throughput
   const double iaxz = t.iaxz[(size_t)a.k * np + col];
   const size_t c0 = (size_t)jj * np + col;
+  const bool lng = is_long(d, i, kk);
   // u1 and u3 on centre jj
-  if (jj == 0 || jj == d.nyu - 1) {
+  const int lu = lev_u(d, lng, jj);
+  if (lu != 1) {  // the column's end rows, or outside a short column
     a.r1[c0] = double2{0.0, 0.0};
     a.r3[c0] = double2{0.0, 0.0};
+    if (lu == 0 || (jj != 0 && jj != d.nyu - 1)) {
+      a.n1[c0] = double2{0.0, 0.0};
+      a.n3[c0] = double2{0.0, 0.0};
+    }
   } else {
     const double a1 = t.d2u[3 * jj], a2 = t.d2u[3 * jj + 1], a3 = t.d2u[3 * jj + 2];
     const double2 pc = ld(a.p + (size_t)(jj - 1) * np + col);
@@ -431,7 +455,9 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
       const double2 A = ld((f == 0 ? a.puu : a.puw) + c0);
       const double2 B = ld((f == 0 ? a.puw : a.pww) + c0);
       const double2* D = f == 0 ? a.puv : a.pvw;
-      const double2 D1 = ld(D + f1), D0 = ld(D + f0);
+      // a short column's product is zero on the middle band's planes (they hold only long modes)
+      const double2 D1 = (lng || !coarse_v(d, jj)) ? ld(D + f1) : double2{0.0, 0.0};
+      const double2 D0 = (lng || !coarse_v(d, jj - 1)) ? ld(D + f0) : double2{0.0, 0.0};
       const double nr = (-kx * A.y - kz * B.y) + c * (D1.x - D0.x);
       const double ni = (kx * A.x + kz * B.x) + c * (D1.y - D0.y);
       (f == 0 ? a.n1 : a.n3)[c0] = double2{nr, ni};
@@ -447,8 +473,10 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
   }
   // u2 on face jj
   if (jj <= d.nyv - 1) {
-    if (jj == 0 || jj == d.nyv - 1) {
+    const int lv = lev_v(d, lng, jj);
+    if (lv != 1) {
       a.r2[c0] = double2{0.0, 0.0};
+      if (lv == 0 || (jj != 0 && jj != d.nyv - 1)) a.n2[c0] = double2{0.0, 0.0};
     } else {
       const double a1 = t.d2v[3 * jj], a2 = t.d2v[3 * jj + 1], a3 = t.d2v[3 * jj + 2];
       const double2 um = ld(a.u2 + c0 - np), u0 = ld(a.u2 + c0), up = ld(a.u2 + c0 + np);
@@ -482,26 +510,17 @@ void launch_assemble(const AsmArgs& a, const Dims& d, const Tables& t, cudaStrea
   k_assemble<<<grid, 256, 0, st>>>(a, d, t);
 }
 
-// Thomas sweeps with the band's shared LU (LUsolU/LUsolV).  One thread per
-// (component, column); levels are prefetched four at a time.
-__global__ void __launch_bounds__(128) k_vsolve(double2* r1, double2* r2, double2* r3, double2* u1, double2* u2,
-                                                double2* u3, Dims d, Tables t, int k) {
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= d.np) return;
-  const int comp = blockIdx.y;
-  const int ny = comp == 1 ? d.nyv : d.nyu;
-  const double* lu = comp == 1 ? t.lu_v + (size_t)k * 3 * d.nyv : t.lu_u + (size_t)k * 3 * d.nyu;
-  const double* a1 = lu;
-  const double* a2 = lu + ny;
-  const double* a3 = lu + 2 * ny;
-  double2* R = comp == 0 ? r1 : (comp == 1 ? r2 : r3);
-  double2* U = comp == 0 ? u1 : (comp == 1 ? u2 : u3);
-  const size_t np = d.np;
-  double2 x = R[col];
-  x = double2{x.x * a2[0], x.y * a2[0]};
-  R[col] = x;
-  int jj = 1;
-  for (; jj + 3 < ny; jj += 4) {
+// Thomas sweeps of one column over levels lo..hi with an LU indexed by level
+// (LUsolU/LUsolV, tridLU_3D_IB.f90:106-116,179-189); levels are prefetched
+// four at a time.
+__device__ __forceinline__ void thomas_column(double2* __restrict__ R, double2* __restrict__ U, size_t np, int col,
+                                              const double* __restrict__ a1, const double* __restrict__ a2,
+                                              const double* __restrict__ a3, int lo, int hi) {
+  double2 x = R[(size_t)lo * np + col];
+  x = double2{x.x * a2[lo], x.y * a2[lo]};
+  R[(size_t)lo * np + col] = x;
+  int jj = lo + 1;
+  for (; jj + 3 <= hi; jj += 4) {
     double2 v[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) v[q] = R[(size_t)(jj + q) * np + col];
@@ -512,14 +531,14 @@ __global__ void __launch_bounds__(128) k_vsolve(double2* r1, double2* r2, double
       R[(size_t)(jj + q) * np + col] = x;
     }
   }
-  for (; jj < ny; ++jj) {
+  for (; jj <= hi; ++jj) {
     const double2 v = R[(size_t)jj * np + col];
     x = double2{(v.x - a1[jj] * x.x) * a2[jj], (v.y - a1[jj] * x.y) * a2[jj]};
     R[(size_t)jj * np + col] = x;
   }
-  U[(size_t)(ny - 1) * np + col] = x;
-  jj = ny - 2;
-  for (; jj - 3 >= 0; jj -= 4) {
+  U[(size_t)hi * np + col] = x;
+  jj = hi - 1;
+  for (; jj - 3 >= lo; jj -= 4) {
     double2 v[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) v[q] = R[(size_t)(jj - q) * np + col];
@@ -530,11 +549,37 @@ __global__ void __launch_bounds__(128) k_vsolve(double2* r1, double2* r2, double
       U[(size_t)(jj - q) * np + col] = x;
     }
   }
-  for (; jj >= 0; --jj) {
+  for (; jj >= lo; --jj) {
     const double2 v = R[(size_t)jj * np + col];
     x = double2{v.x - a3[jj] * x.x, v.y - a3[jj] * x.y};
     U[(size_t)jj * np + col] = x;
   }
+}
+
+// Velocity solves: one thread per (component, column).  Long columns use the
+// LU of the whole channel; short columns solve their two wall bands with those
+// bands' LUs and are zero in between.
+__global__ void __launch_bounds__(128) k_vsolve(double2* r1, double2* r2, double2* r3, double2* u1, double2* u2,
+                                                double2* u3, Dims d, Tables t, int k) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= d.np) return;
+  const int comp = blockIdx.y;
+  const int ny = comp == 1 ? d.nyv : d.nyu;
+  double2* R = comp == 0 ? r1 : (comp == 1 ? r2 : r3);
+  double2* U = comp == 0 ? u1 : (comp == 1 ? u2 : u3);
+  const size_t np = d.np;
+  const int i = col % d.nkx, kk = col / d.nkx;
+  if (is_long(d, i, kk)) {
+    const double* lu = comp == 1 ? t.lu_v + (size_t)k * 3 * d.nyv : t.lu_u + (size_t)k * 3 * d.nyu;
+    thomas_column(R, U, np, col, lu, lu + ny, lu + 2 * ny, 0, ny - 1);
+    return;
+  }
+  const double* l1 = (comp == 1 ? t.lu_v1 : t.lu_u1) + (size_t)k * 3 * ny;
+  const double* l3 = (comp == 1 ? t.lu_v3 : t.lu_u3) + (size_t)k * 3 * ny;
+  const int e1 = comp == 1 ? d.Nv1 + 1 : d.Nu1 + 1, s3 = comp == 1 ? d.Nv2 : d.Nu2;
+  thomas_column(R, U, np, col, l1, l1 + ny, l1 + 2 * ny, 0, e1);
+  thomas_column(R, U, np, col, l3, l3 + ny, l3 + 2 * ny, s3, ny - 1);
+  for (int jj = e1 + 1; jj < s3; ++jj) U[(size_t)jj * np + col] = double2{0.0, 0.0};
 }
 
 void launch_vsolve(double2* r1, double2* r2, double2* r3, double2* u1, double2* u2, double2* u3, const Dims& d,
@@ -571,29 +616,40 @@ void launch_flowrate(double2* u1, DevScalars* sc, const Dims& d, const Tables& t
 // LU_buildP + LU_decP (tridLU_3D_IB.f90:497-571,643-684), one thread per
 // column.  rows holds, per p level, the six products the matrix is made of:
 // [0] D_b(j-1)*G_t(j)  [1] D_t(j)*G_b(j)  [2] D_b(j-1)*G_b(j-1)  [3] D_t(j)*G_t(j+1).
+// LU_buildP + LU_decP (tridLU_3D_IB.f90:497-571,643-684) of one column over
+// its p levels s0..e (rows: the column-independent D G products per level).
+__device__ __forceinline__ void build_dg_segment(double* dg2, double* dg3, const double* rows, size_t np, int col,
+                                                 double k2, bool dirichlet, double pin, int s0, int e) {
+  double a2 = rows[4 * (size_t)s0 + 1] + k2;
+  double a3 = rows[4 * (size_t)s0 + 3];
+  if (dirichlet) { a2 = pin; a3 = 0.0; }
+  a2 = 1.0 / a2;
+  dg2[(size_t)s0 * np + col] = a2;
+  for (int jp = s0 + 1; jp <= e; ++jp) {
+    a3 = a3 * a2;                       // scaled upper diagonal of row jp-1
+    dg3[(size_t)(jp - 1) * np + col] = a3;
+    const double* q = rows + 4 * (size_t)jp;
+    const double b2 = (jp < e) ? (q[0] + q[1]) + k2 : q[0] + k2;
+    a2 = 1.0 / (b2 - q[2] * a3);
+    dg2[(size_t)jp * np + col] = a2;
+    a3 = (jp < e) ? q[3] : 0.0;
+  }
+  dg3[(size_t)e * np + col] = 0.0;
+}
+
 __global__ void k_build_dg(double* dg2, double* dg3, const double* rows, Dims d, Tables t, double pin) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= d.np) return;
   const int i = col % d.nkx, kk = col / d.nkx;
-  const double k2x = t.k2x[i], k2z = t.k2z[kk];
-  const int ne = d.nyp - 1;
+  const double k2 = t.k2x[i] + t.k2z[kk];
   const size_t np = d.np;
-  // first row
-  double a2 = rows[1] + k2x + k2z;
-  double a3 = rows[3];
-  if (col == 0) { a2 = pin; a3 = 0.0; }
-  a2 = 1.0 / a2;
-  dg2[col] = a2;
-  for (int jp = 1; jp <= ne; ++jp) {
-    a3 = a3 * a2;                       // scaled upper diagonal of row jp-1
-    dg3[(size_t)(jp - 1) * np + col] = a3;
-    const double* q = rows + 4 * (size_t)jp;
-    const double b2 = (jp < ne) ? (q[0] + q[1]) + k2x + k2z : q[0] + k2x + k2z;
-    a2 = 1.0 / (b2 - q[2] * a3);
-    dg2[(size_t)jp * np + col] = a2;
-    a3 = (jp < ne) ? q[3] : 0.0;
+  if (is_long(d, i, kk)) {
+    // mode (0,0): Dirichlet row for psi (tridLU_3D_IB.f90:548-554)
+    build_dg_segment(dg2, dg3, rows, np, col, k2, col == 0, pin, 0, d.nyp - 1);
+  } else {  // short column: its two wall bands, Neumann-like ends at the band edges
+    build_dg_segment(dg2, dg3, rows, np, col, k2, false, pin, 0, d.Nu1 - 1);
+    build_dg_segment(dg2, dg3, rows, np, col, k2, false, pin, d.Nu2, d.nyp - 1);
   }
-  dg3[(size_t)ne * np + col] = 0.0;
 }
 
 void launch_build_dg(double* dg2, double* dg3, const double* rows, const Dims& d, const Tables& t, double pin,
@@ -601,27 +657,25 @@ void launch_build_dg(double* dg2, double* dg3, const double* rows, const Dims& d
   k_build_dg<<<(d.np + 127) / 128, 128, 0, st>>>(dg2, dg3, rows, d, t, pin);
 }
 
-// solveP + v_corr per column.
-__global__ void __launch_bounds__(128) k_psolve(double2* u1, double2* u2, double2* u3, double2* p, double2* psi,
-                                                Dims d, Tables t, double dtirk, double dtrk, double gwb,
-                                                double gwt) {
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= d.np) return;
+// solveP + v_corr over the p levels lo..hi of one column (a long column's all,
+// or one wall band of a short one).  The divergence is formed on the fly in
+// the forward sweep; the backward sweep adds psi to p and corrects u, w on the
+// same levels and v on the faces between them.
+__device__ __forceinline__ void psolve_segment(double2* u1, double2* u2, double2* u3, double2* p, double2* psi,
+                                               const Dims& d, const Tables& t, int col, double kx, double kz,
+                                               double dtirk, double dtrk, int lo, int hi, bool pin00) {
   const size_t np = d.np;
-  const int i = col % d.nkx, kk = col / d.nkx;
-  const double kx = t.kx[i], kz = t.kz[kk];
-  const int nyp = d.nyp;
   double2 x = double2{0.0, 0.0};
-  for (int jp = 0; jp < nyp; ++jp) {
+  for (int jp = lo; jp <= hi; ++jp) {
     const int ju = jp + 1;
     const double2 a = u1[(size_t)ju * np + col], w = u3[(size_t)ju * np + col];
     const double2 v1 = u2[(size_t)ju * np + col], v0 = u2[(size_t)jp * np + col];
     const double c = t.cu[ju];
     double2 dv = double2{(-kx * a.y - kz * w.y) + c * (v1.x - v0.x), (kx * a.x + kz * w.x) + c * (v1.y - v0.y)};
     double2 ps = double2{dtirk * dv.x, dtirk * dv.y};
-    if (col == 0 && jp == 0) ps = double2{0.0, 0.0};
+    if (pin00 && jp == lo) ps = double2{0.0, 0.0};
     const double b2 = t.dg2[(size_t)jp * np + col];
-    if (jp == 0) x = double2{ps.x * b2, ps.y * b2};
+    if (jp == lo) x = double2{ps.x * b2, ps.y * b2};
     else {
       const double b1 = t.dg1[jp];
       x = double2{(ps.x - b1 * x.x) * b2, (ps.y - b1 * x.y) * b2};
@@ -629,10 +683,10 @@ __global__ void __launch_bounds__(128) k_psolve(double2* u1, double2* u2, double
     psi[(size_t)jp * np + col] = x;
   }
   const double kxd = dtrk * kx, kzd = dtrk * kz;
-  double2 xn = x;  // psi(nyp-1)
-  for (int jp = nyp - 1; jp >= 0; --jp) {
+  double2 xn = x;  // psi(hi)
+  for (int jp = hi; jp >= lo; --jp) {
     double2 xc;
-    if (jp == nyp - 1) xc = xn;
+    if (jp == hi) xc = xn;
     else {
       const double2 v = psi[(size_t)jp * np + col];
       const double b3 = t.dg3[(size_t)jp * np + col];
@@ -645,12 +699,31 @@ __global__ void __launch_bounds__(128) k_psolve(double2* u1, double2* u2, double
     u1[cu] = double2{a.x - (-kxd * xc.y), a.y - (kxd * xc.x)};
     double2 w = u3[cu];
     u3[cu] = double2{w.x - (-kzd * xc.y), w.y - (kzd * xc.x)};
-    if (jp <= nyp - 2) {
+    if (jp < hi) {
       const double f = dtrk * t.cv[jp + 1];
       double2 v = u2[cu];
       u2[cu] = double2{v.x - f * (xn.x - xc.x), v.y - f * (xn.y - xc.y)};
     }
     xn = xc;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_psolve(double2* u1, double2* u2, double2* u3, double2* p, double2* psi,
+                                                Dims d, Tables t, double dtirk, double dtrk, double gwb,
+                                                double gwt) {
+  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= d.np) return;
+  const size_t np = d.np;
+  const int i = col % d.nkx, kk = col / d.nkx;
+  const double kx = t.kx[i], kz = t.kz[kk];
+  if (is_long(d, i, kk)) {
+    psolve_segment(u1, u2, u3, p, psi, d, t, col, kx, kz, dtirk, dtrk, 0, d.nyp - 1, col == 0);
+  } else {
+    psolve_segment(u1, u2, u3, p, psi, d, t, col, kx, kz, dtirk, dtrk, 0, d.Nu1 - 1, false);
+    psolve_segment(u1, u2, u3, p, psi, d, t, col, kx, kz, dtirk, dtrk, d.Nu2, d.nyp - 1, false);
+    // v on the end rows of the short column's bands (v_corr, littleharsh.f90:904-905)
+    u2[(size_t)(d.Nv1 + 1) * np + col] = double2{0.0, 0.0};
+    u2[(size_t)d.Nv2 * np + col] = double2{0.0, 0.0};
   }
   u2[col] = double2{0.0, 0.0};
   u2[(size_t)(d.nyv - 1) * np + col] = double2{0.0, 0.0};
@@ -676,6 +749,7 @@ __global__ void k_divergence(const double2* u1, const double2* u2, const double2
   const int jp = blockIdx.y, ju = jp + 1;
   const size_t np = d.np;
   const int i = col % d.nkx, kk = col / d.nkx;
+  if (!lev_p(d, is_long(d, i, kk), jp)) { div[(size_t)jp * np + col] = double2{0.0, 0.0}; return; }
   const double kx = t.kx[i], kz = t.kz[kk];
   const double2 a = u1[(size_t)ju * np + col], w = u3[(size_t)ju * np + col];
   const double2 v1 = u2[(size_t)ju * np + col], v0 = u2[(size_t)jp * np + col];
@@ -767,12 +841,14 @@ __global__ void k_spectra(const double2* u1, const double2* u2, const double2* u
 // into -N2/2 and +N2/2 on the padded grid).  sum f = Ngx Ngz Re f(0,0).
 // acc rows (length L = max(nyu, nyv)): 0 Um 1 U2m 2 Vm 3 V2m 4 Wm 5 W2m 6 Pm 7 P2m
 // 8 UVm (u, v at centres) 9 UWm 10 VWm (v, w at faces).  One block per level.
+// With bands a plane of the middle band sums over its own points: only the long
+// columns count, the lone mode is that band's -N2/2 and the factor its Ngx Ngz.
 __device__ __forceinline__ double pair_term(const double2* f, const double2* g, int col, int i, int kk, int nz,
-                                            int nkx) {
+                                            int nkx, int lone) {
   const double2 a = f[col], b = g[col];
   const double re = a.x * b.x + a.y * b.y;  // Re(a conj b)
   if (i > 0) return 2.0 * re;
-  if (kk == nz / 2) return 0.5 * re;
+  if (kk == lone) return 0.5 * re;
   const int pk = (nz - kk) % nz;
   const double2 c = g[(size_t)pk * nkx];
   return 0.5 * (re + (a.x * c.x - a.y * c.y));  // + Re(a g(-kz))
@@ -810,19 +886,25 @@ __global__ void __launch_bounds__(256) k_stats(const double2* u1, const double2*
   const double2* W = u3 + (size_t)jj * np;
   const double2* V = u2 + (size_t)jj * np;
   const double2* P = p + (size_t)jj * np;
+  // plane of each group: u quantities at centre jj, v ones at face jj, p at p level jj (centre jj + 1)
+  const bool cu_ = coarse_u(d, jj), cv_ = coarse_v(d, jj), cp_ = coarse_u(d, jj + 1);
+  const int lone_f = d.nz / 2, lone_c = d.nz - d.nz2 / 2;
   for (int col = threadIdx.x; col < d.np; col += blockDim.x) {
     const int i = col % d.nkx, kk = col / d.nkx;
-    if (jj < d.nyu) {
-      s[1] += pair_term(U, U, col, i, kk, d.nz, d.nkx);
-      s[5] += pair_term(W, W, col, i, kk, d.nz, d.nkx);
-      s[8] += pair_term(U, vcl, col, i, kk, d.nz, d.nkx);
-      s[9] += pair_term(U, W, col, i, kk, d.nz, d.nkx);
+    const bool lng = is_long(d, i, kk);
+    if (jj < d.nyu && (lng || !cu_)) {
+      const int lone = cu_ ? lone_c : lone_f;
+      s[1] += pair_term(U, U, col, i, kk, d.nz, d.nkx, lone);
+      s[5] += pair_term(W, W, col, i, kk, d.nz, d.nkx, lone);
+      s[8] += pair_term(U, vcl, col, i, kk, d.nz, d.nkx, lone);
+      s[9] += pair_term(U, W, col, i, kk, d.nz, d.nkx, lone);
     }
-    if (jj < d.nyv) {
-      s[3] += pair_term(V, V, col, i, kk, d.nz, d.nkx);
-      s[10] += pair_term(V, wfl, col, i, kk, d.nz, d.nkx);
+    if (jj < d.nyv && (lng || !cv_)) {
+      const int lone = cv_ ? lone_c : lone_f;
+      s[3] += pair_term(V, V, col, i, kk, d.nz, d.nkx, lone);
+      s[10] += pair_term(V, wfl, col, i, kk, d.nz, d.nkx, lone);
     }
-    if (jj < d.nyp) s[7] += pair_term(P, P, col, i, kk, d.nz, d.nkx);
+    if (jj < d.nyp && (lng || !cp_)) s[7] += pair_term(P, P, col, i, kk, d.nz, d.nkx, cp_ ? lone_c : lone_f);
   }
   if (threadIdx.x == 0) {
     if (jj < d.nyu) { s[0] = U[0].x; s[4] = W[0].x; }
@@ -840,8 +922,10 @@ __global__ void __launch_bounds__(256) k_stats(const double2* u1, const double2*
   if (threadIdx.x < 11) {
     double x = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) x += red[w][threadIdx.x];
-    const double scale = (double)d.ngx * (double)d.ngz;
-    acc[(size_t)threadIdx.x * L + jj] += scale * x;
+    const int r = threadIdx.x;
+    const bool coarse = (r == 2 || r == 3 || r == 10) ? cv_ : ((r == 6 || r == 7) ? cp_ : cu_);
+    const double scale = coarse ? (double)d.ngx2 * (double)d.ngz2 : (double)d.ngx * (double)d.ngz;
+    acc[(size_t)r * L + jj] += scale * x;
   }
 }
 

@@ -91,6 +91,8 @@ extern "C" int lh_project_noalloc(const lh_params* prm, const double* yu, const 
   d.nz = nz;
   d.np = d.nkx * nz;
   d.mp = d.nkx * d.ngz;
+  d.spitch = d.nkx;
+  d.snz = nz;
   d.ju0 = Nf(4, 0);
   d.nyu = Nf(4, 3) + 1 - Nf(4, 0) + 1;
   d.nyv = Nf(3, 3) + 1 - Nf(3, 0) + 1;

@@ -54,8 +54,9 @@ def layer_shapes(nblocks: int = NBLOCKS):
 
 def init_params(seed: int = 0, nblocks: int = NBLOCKS):
     """He-initialised fp32 weights [27][cout][cin] and zero biases (numpy).
-    The second convolution of each block and the tail start small so the
-    untrained network is close to the identity correction (zero)."""
+    The second convolution of each block starts small and the tail at zero,
+    so the untrained network's correction is exactly zero and each block
+    starts close to the identity."""
     rng = np.random.default_rng(seed)
     out = []
     shapes = layer_shapes(nblocks)
@@ -65,7 +66,7 @@ def init_params(seed: int = 0, nblocks: int = NBLOCKS):
             std *= 0.1
         w = (rng.standard_normal((27, co, ci)) * std).astype(np.float32)
         if i == len(shapes) - 1:
-            w[:, 3:, :] = 0.0  # unused output channels stay zero
+            w[:] = 0.0  # zero correction at the start; unused output channels stay zero for good
         out.append((w, np.zeros(co, np.float32)))
     return out
 
@@ -105,6 +106,7 @@ class SRNet:
         self.flip = [torch.zeros(27 * vw["ci"] * vw["co"], dtype=torch.bfloat16, device=dev) for vw in self.views]
         self.lr, self.betas, self.eps, self.wd = lr, betas, eps, weight_decay
         self.t = 0
+        self.sigma = 1.0  # scale of the correction (set by training: rms of the residual it learns)
         self._acts = None
         self._shape = None
 
@@ -117,12 +119,13 @@ class SRNet:
         return out
 
     def state_dict(self):
-        return {"master": self.master.cpu().numpy(), "nblocks": self.nblocks}
+        return {"master": self.master.cpu().numpy(), "nblocks": self.nblocks, "sigma": self.sigma}
 
-    def load_state(self, master: np.ndarray):
+    def load_state(self, state: dict):
         torch = _torch()
-        self.master.copy_(torch.from_numpy(np.asarray(master, np.float32)).cuda())
+        self.master.copy_(torch.from_numpy(np.asarray(state["master"], np.float32)).cuda())
         self.wb16.copy_(self.master.to(torch.bfloat16))
+        self.sigma = float(state.get("sigma", 1.0))
 
     # -- kernels ------------------------------------------------------------------
     def _conv(self, li, x, out, res=None, gate=None, flags=BIAS, out_f32=False, weights=None, cin=None, cout=None):

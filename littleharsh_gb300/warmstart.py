@@ -226,35 +226,51 @@ def mse_of(a, b) -> float:
     return float(((a.double() - b.double()) ** 2).mean())
 
 
+def residual_scale(pairs: PairSet, idx) -> float:
+    """rms of target - base over the pairs idx: the network predicts the
+    residual in these units, so its output and the loss are O(1)."""
+    acc, n = 0.0, 0
+    for i in idx:
+        d = (pairs.target[i] - pairs.base[i]).double()
+        acc += float((d * d).sum())
+        n += d.numel()
+    return math.sqrt(acc / max(n, 1)) if acc > 0 else 1.0
+
+
 def train(net, pairs: PairSet, train_idx, val_idx, epochs: int = 10, lr: float = 1e-3, seed: int = 0, log=None):
-    """AdamW over the training pairs (one pair per step), cosine learning rate.
-    Returns the history: per epoch the mean training loss and the validation
-    MSE of the network against that of the lifted field alone."""
+    """AdamW over the training pairs (one pair per step), cosine learning rate,
+    on the residual target - base scaled by its rms (kept in net.sigma).
+    Returns the history: per epoch the mean training loss (scaled units) and
+    the validation MSE of the corrected field against that of the lifted field
+    alone (physical units)."""
     torch = _torch()
     rng = np.random.default_rng(seed)
+    net.sigma = residual_scale(pairs, train_idx)
     hist = []
     nsteps = epochs * len(train_idx)
     step = 0
     loss_acc = torch.zeros(1, dtype=torch.float64, device="cuda")
+    zero = torch.zeros_like(pairs.base[train_idx[0]])
     t0 = time.perf_counter()
     for ep in range(epochs):
         order = rng.permutation(train_idx)
         loss_acc.zero_()
         for i in order:
             cur = lr * 0.5 * (1.0 + math.cos(math.pi * step / max(nsteps, 1)))
+            tgt = ((pairs.target[i] - pairs.base[i]) * (1.0 / net.sigma)).contiguous()
             net.zero_grad()
             corr = net.forward(pairs.x[i], keep=True)
-            dcorr = net.loss_grad(corr, pairs.base[i], pairs.target[i], loss_acc)
+            dcorr = net.loss_grad(corr, zero, tgt, loss_acc)
             net.backward(dcorr)
             net.adam_step(cur)
             step += 1
         torch.cuda.synchronize()
         tr = loss_acc.item() / max(len(order), 1)
         v_net, v_lift = evaluate(net, pairs, val_idx)
-        hist.append({"epoch": ep + 1, "train_mse": tr, "val_mse_net": v_net, "val_mse_lifted": v_lift,
+        hist.append({"epoch": ep + 1, "train_loss_scaled": tr, "val_mse_net": v_net, "val_mse_lifted": v_lift,
                      "seconds": time.perf_counter() - t0})
         if log:
-            log(f"epoch {ep + 1}: train {tr:.4e}  val net {v_net:.4e}  val lifted {v_lift:.4e}  "
+            log(f"epoch {ep + 1}: train {tr:.4e} (scaled)  val net {v_net:.4e}  val lifted {v_lift:.4e}  "
                 f"({time.perf_counter() - t0:.1f} s)")
     return hist
 
@@ -265,9 +281,10 @@ def evaluate(net, pairs: PairSet, idx):
     if len(idx) == 0:
         return float("nan"), float("nan")
     a, b = 0.0, 0.0
+    sig = getattr(net, "sigma", 1.0)
     for i in idx:
         corr = net.forward(pairs.x[i])
-        pred = pairs.base[i] + corr.reshape(-1, 16)[:, :3]
+        pred = pairs.base[i] + sig * corr.reshape(-1, 16)[:, :3]
         a += mse_of(pred, pairs.target[i])
         b += mse_of(pairs.base[i], pairs.target[i])
     torch.cuda.synchronize()
@@ -282,7 +299,7 @@ def warm_field(net, cu1, cu2, cu3, coarse: GridInfo, fine: GridInfo, use_net: bo
         return [f.cpu().numpy() for f in lifted]
     base = to_volume(*lifted, fine)
     corr = net.forward(net_input(base, fine))
-    vol = base + corr[..., :3]
+    vol = base + getattr(net, "sigma", 1.0) * corr[..., :3]
     return [f.cpu().numpy() for f in from_volume(vol, fine)]
 
 

@@ -30,11 +30,12 @@ def test_pairs_training_and_start():
     b, t = pairs.base[0], pairs.target[0]
     err = ws.mse_of(b, t)
     assert 0.0 < err < 0.05 * float((t.double() ** 2).mean())
-    net = SRNet(seed=0, lr=3e-3)
+    net = SRNet(seed=0)
     v0 = ws.evaluate(net, pairs, [0, 1])
-    ws.train(net, pairs, [0, 1], [2], epochs=15, lr=3e-3)
+    assert v0[0] == pytest.approx(v0[1], rel=1e-6)  # the untrained correction is zero
+    ws.train(net, pairs, [0, 1], [2], epochs=20, lr=1e-3)
     v1 = ws.evaluate(net, pairs, [0, 1])
-    assert v1[0] < v0[0], (v0, v1)  # training lowers the loss on the pairs it was trained on
+    assert v1[0] < 0.9 * v0[0], (v0, v1)  # training lowers the error on the pairs it was trained on
     assert abs(v1[1] - v0[1]) < 1e-12  # the lifted fields are untouched
     # the start: coarse field -> lifted + corrected -> projected -> steps
     coarse = lh.Solver(lh.Config(**CONFIG1_COARSE))

