@@ -31,10 +31,11 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-from littleharsh_gb300.workloads import CONFIG1, CONFIG2, MID288, ensemble_configs  # noqa: E402
+from littleharsh_gb300.workloads import CONFIG1, CONFIG2, CONFIG2_BANDS, MID288, ensemble_configs  # noqa: E402
 
 WORKLOADS = {
     "config2_576x576x450_fp64": CONFIG2,
+    "config2_bands_576_384x450_fp64": CONFIG2_BANDS,
     "config1_96x96x130_fp64": CONFIG1,
     "mid_288x288x226_fp64": MID288,
 }
@@ -164,6 +165,19 @@ def z_flops(ngz, nkx, nplanes, prune_last=False) -> float:
 
 
 # ----------------------------------------------------------------------------
+def grid_points(cfg: dict, nyu: int, N) -> int:
+    """Physical collocation points of one field: Ngalx * Ngalz per u level, the
+    middle band's own Ngalx2 * Ngalz2 on its levels N(4,1)+1..N(4,2) when the
+    workload has variable-resolution bands.  N is the lh_params N array
+    (N(r, b) at [4 b + r - 1])."""
+    fine = cfg["ngalx"] * cfg["ngalz"]
+    if not cfg.get("ngalx2") and not cfg.get("ngalz2"):
+        return fine * nyu
+    coarse = (cfg.get("ngalx2") or cfg["ngalx"]) * (cfg.get("ngalz2") or cfg["ngalz"])
+    nmid = N[2 * 4 + 3] - N[1 * 4 + 3]
+    return fine * (nyu - nmid) + coarse * nmid
+
+
 def max_over_ranks(value: float, dist, device: str) -> float:
     """The slowest rank's timing (replicas only: no data moves between ranks)."""
     if dist is None:
@@ -206,8 +220,8 @@ def cpu_baseline(cfg: dict, threads: int) -> dict:
     t0 = time.perf_counter()
     o.step(1)
     sec = time.perf_counter() - t0
-    pts = o.ngx * o.ngz * o.nyu
-    return {"value": pts / sec, "unit": UNIT, "cores": threads, "kind": "port",
+    pts = grid_points(cfg, o.nyu, [x for b in range(5) for x in (o.sz.N[0][b], o.sz.N[1][b], o.sz.N[2][b], o.sz.N[3][b])])
+    return {"value": pts / sec, "unit": UNIT, "cores": threads, "kind": "port", "points": pts,
             "sample": f"1 RK3 step of {cfg['ngalx']}x{cfg['ngalz']}x{o.nyu} FP64 ({sec:.1f} s)"}
 
 
@@ -225,7 +239,7 @@ def run_reference(args, rank: int, world: int):
         vals.append(base["value"])
     v = statistics.median(vals)
     base["value"] = v
-    pts = cfg["ngalx"] * cfg["ngalz"] * (cfg["ny"] + 2 * cfg["dsty"] + 1)
+    pts = base["points"]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": len(vals),
             "warmup": args.warmup, "ms_per_step": 1e3 * pts / v, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded laminar + perturbation field)",
@@ -277,7 +291,7 @@ def run_ours(args, rank: int, world: int, local_rank: int, dist):
     cfg = WORKLOADS[args.workload]
     prec = lh.PREC_MIXED if args.precision == "mixed" else lh.PREC_FP64
     s, ic = build_solver(cfg, prec, seed=1 + rank)
-    pts = s.ngx * s.ngz * s.nyu
+    pts = grid_points(cfg, s.nyu, list(s.params.N))
     if args.warmup > 0:
         s.step(args.warmup)
 

@@ -17,6 +17,10 @@ CONFIG1 = dict(Re=2800.0, alp=1.0, bet=2.0, ngalx=96, ngalz=96, ny=97, dyq=13.6,
 CONFIG2 = dict(Re=10000.0, alp=1.0, bet=2.0, ngalx=576, ngalz=576, ny=385, dyq=13.6, ppp=5, geometry_type=3,
                posth=0.1, dsty=32, dstx=8, dstz=8, ntilex=48, ntilez=24, flag_ctpress=0)
 
+# configuration 2 with the reference's variable-resolution bands: the middle band
+# (between the canopy layers) at 384 x 384 points (256 x 256 modes)
+CONFIG2_BANDS = dict(CONFIG2, ngalx2=384, ngalz2=384)
+
 # mid-size case for profiler captures: x-pass inputs larger than L2, ~2 GB on the device
 MID288 = dict(Re=5000.0, alp=1.0, bet=2.0, ngalx=288, ngalz=288, ny=193, dyq=13.6, ppp=5, geometry_type=3, posth=0.1,
               dsty=16, dstx=4, dstz=4, ntilex=24, ntilez=12, flag_ctpress=0)
