@@ -203,6 +203,7 @@ def build_solver(cfg: dict, precision: int, seed: int):
     s.project()
     dt = s.cfl_dt(0.5)
     s.set_time(0.0, dt, 0.0)
+    s.tuned = s.autotune()  # launch shapes picked by timing on this grid (lh_autotune)
     return s, (u1, u2, u3, p)
 
 
@@ -378,8 +379,11 @@ def run_ours(args, rank: int, world: int, local_rank: int, dist):
                "data": "synthetic (seeded laminar + 10% perturbation, projected divergence-free)",
                "config": {"workload": args.workload, "grid_phys": [s.ngx, s.ngz, s.nyu],
                           "modes": [2 * (s.nkx - 1), s.nz], "spectral_points": s.nkx * s.nz * s.nyu,
-                          "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (534 MB per field)",
-                          "precision": args.precision},
+                          "parallelism": f"replicas x{world}",
+                          "l2": f"inputs larger than L2 ({16 * s.nkx * s.nz * s.nyu / 1e6:.0f} MB per field)",
+                          "precision": args.precision, "launch_shapes": getattr(s, "tuned", None),
+                          "bands": [cfg.get("ngalx2") or cfg["ngalx"], cfg.get("ngalz2") or cfg["ngalz"]]
+                          if cfg.get("ngalx2") else None},
                "gpu_launches": launches * args.steps, "e2e": e2e, "roofline": roof, "kernels_ms_per_step": kernels,
                "clocks": clocks}
         if not args.no_cpu_baseline and world == 1:
@@ -417,7 +421,10 @@ def run_srnet(args):
     out = {"metric": "SR network bf16 TFLOP/s", "unit": "TFLOP/s", "higher_is_better": True, "n_gpus": 1,
            "dtype": "bf16 (fp32 accumulate)", "kernel": "mma.sync m16n8k16 implicit-GEMM 3x3x3 conv"}
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
-    for name, cfg, train in (("train_step_config1", CONFIG1, True), ("inference_config5_fine", CONFIG5_FINE, False)):
+    cases = [("train_step_config1", CONFIG1, True), ("inference_config5_fine", CONFIG5_FINE, False)]
+    if args.sr_small:  # profiler captures: the configuration-1 training step only
+        cases = cases[:1]
+    for name, cfg, train in cases:
         gi = ws.GridInfo.from_config(cfg)
         Y, Z, X = gi.nyu, gi.ngz, gi.ngx
         g = torch.Generator(device="cuda").manual_seed(0)
@@ -452,6 +459,8 @@ def run_srnet(args):
         del x, base, tgt
         torch.cuda.empty_cache()
     out["value"] = out["train_step_config1"]["tflops"]
+    if "inference_config5_fine" not in out:
+        out["note"] = "configuration-1 training step only (--sr-small)"
     out["peak_bf16_tflops"] = peaks.get("bf16_tflops")
     print(json.dumps(out), flush=True)
 
@@ -467,6 +476,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ensemble", action="store_true", help="configuration 4: 16 replicas in one graph per step")
     ap.add_argument("--srnet", action="store_true", help="the warm start's network kernels (training and inference)")
+    ap.add_argument("--sr-small", action="store_true", help="with --srnet: the configuration-1 training step only")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -196,6 +196,15 @@ int lh_last_step_ms(lh_handle* h, double* ms, int32_t* launches_per_step);
  * nkinds must be at least 10. */
 int lh_profile_step(lh_handle* h, double* ms_by_kind, int32_t* count_by_kind, int32_t nkinds);
 
+/* Launch-shape autotuner (no reference counterpart).  Times the z passes for
+ * each z tile width (columns per CTA) and the product pass for each number of
+ * levels per CTA on this handle's grid and precision, keeps the fastest of
+ * each and returns them (either pointer may be NULL).  Needs fields; writes
+ * only scratch, so the fields and the time are unchanged.  The next step is
+ * captured with the new shapes. */
+int lh_autotune(lh_handle* h, int32_t* tx, int32_t* chunk);
+
+
 /* Divergence-free projection (solveP + v_corr with kRK = 1, the operation of
  * lh_project) of caller-owned device arrays u1, u2, u3 (plane layout), for
  * callers that cannot allocate device memory: a Fortran driver whose fields

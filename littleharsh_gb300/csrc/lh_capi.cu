@@ -333,21 +333,21 @@ int band_launches(const lh_handle* h, BandLaunch* out) {
   return 3;
 }
 
+// The nonlinear term's plane work, one band at a time (one band without
+// variable resolution): z-inverse of the levels the band's products need,
+// products, z-forward of the band's product planes.  The flags select parts
+// (the autotuner times them separately); a substage runs all three.
 template <typename R>
-int enqueue_substage(lh_handle* h, int k, int upto) {
+void enqueue_nonlinear(lh_handle* h, cudaStream_t st, bool zinv, bool xprod, bool zfwd) {
   using T2 = cpx_t<R>;
   const Dims& d = h->d;
-  cudaStream_t st = h->st;
-  const double beta = h->bRK[k] * h->dt / h->Re;
-  // nonlinear, one band at a time (one band without variable resolution): z-inverse of the levels the
-  // band's products need, products, z-forward of the band's product planes
   BandLaunch bl[3];
   const int nbl = band_launches(h, bl);
   for (int b = 0; b < nbl; ++b) {
     const BandLaunch& B = bl[b];
     const Dims& db = *B.d;
     const int L0 = std::min(B.c_lo, B.f_lo + 1), L1 = std::max(B.c_hi, B.f_hi + 1);
-    {
+    if (zinv) {
       const int ul = std::max(1, L0 - 1), uh = std::min(d.nyu - 2, L1);
       const int vl = std::max(1, L0 - 1), vh = std::min(d.nyv - 2, L1);
       ZJobs<R> J{};
@@ -359,7 +359,7 @@ int enqueue_substage(lh_handle* h, int k, int upto) {
       launch_zinv<R>(J, db, *B.pz, h->tx, st);
       mark(h, K_ZINV);
     }
-    {
+    if (xprod) {
       ProdArgs<R> a{};
       a.mu = (const T2*)h->mixu;
       a.mw = (const T2*)h->mixw;
@@ -372,7 +372,7 @@ int enqueue_substage(lh_handle* h, int k, int upto) {
       launch_xprod<R>(a, db, *B.ph, *B.pf, B.rtw, st);
       mark(h, K_XPROD);
     }
-    {
+    if (zfwd) {
       ZJobs<R> J{};
       double2* outs[6] = {h->puu, h->puw, h->pww, h->pvv, h->puv, h->pvw};
       for (int i = 0; i < 6; ++i) {
@@ -385,6 +385,32 @@ int enqueue_substage(lh_handle* h, int k, int upto) {
       mark(h, K_ZFWD);
     }
   }
+}
+
+// One timed pass of the autotuner: the z passes and/or the product pass of the
+// nonlinear term, best of two, in milliseconds (negative on a CUDA error).
+template <typename R>
+float time_parts(lh_handle* h, bool z, bool x, cudaEvent_t e0, cudaEvent_t e1) {
+  float best = 1e30f;
+  for (int rep = 0; rep < 2; ++rep) {
+    cudaEventRecord(e0, h->st);
+    enqueue_nonlinear<R>(h, h->st, z, x, z);
+    cudaEventRecord(e1, h->st);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return -1.f;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = std::min(best, ms);
+  }
+  return best;
+}
+
+template <typename R>
+int enqueue_substage(lh_handle* h, int k, int upto) {
+  using T2 = cpx_t<R>;
+  const Dims& d = h->d;
+  cudaStream_t st = h->st;
+  const double beta = h->bRK[k] * h->dt / h->Re;
+  enqueue_nonlinear<R>(h, st, true, true, true);
   {
     AsmArgs a{};
     a.u1 = h->u1; a.u2 = h->u2; a.u3 = h->u3; a.p = h->p;
@@ -1110,6 +1136,54 @@ int lh_last_step_ms(lh_handle* h, double* ms, int32_t* launches) {
   if (!h) return LH_EINVAL;
   if (ms) *ms = h->last_ms;
   if (launches) *launches = h->launches_per_step;
+  return LH_OK;
+}
+
+// Launch-shape autotuner: the z passes' tile width (columns per CTA) and the
+// product pass's levels per CTA, each picked as the fastest of its candidates
+// on this handle's grid and precision.  Only scratch buffers are written
+// (mixed planes, product spectra), so the fields are untouched.
+int lh_autotune(lh_handle* h, int32_t* tx_out, int32_t* chunk_out) {
+  if (!h) return LH_EINVAL;
+  if (!h->have_fields) return fail(h, LH_ESTATE, "fields must be set first");
+  cudaSetDevice(h->device);
+  CU(h, cudaStreamSynchronize(h->st));
+  int optin = 0;
+  CU(h, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+  const size_t elem = h->precision == LH_PREC_MIXED ? sizeof(float2) : sizeof(double2);
+  cudaEvent_t e0, e1;
+  CU(h, cudaEventCreate(&e0));
+  CU(h, cudaEventCreate(&e1));
+  const int tx0 = h->tx, ch0 = h->chunk;
+  int best_tx = tx0, best_ch = ch0;
+  float best = 1e30f;
+  for (int tx : {1, 2, 4, 8, 16, 32}) {
+    if ((size_t)h->d.ngz * tx * elem > (size_t)optin - 1024) continue;  // the z tile must fit in shared memory
+    h->tx = tx;
+    const float ms = h->precision == LH_PREC_MIXED ? time_parts<float>(h, true, false, e0, e1)
+                                                   : time_parts<double>(h, true, false, e0, e1);
+    if (ms < 0.f) { h->tx = tx0; cudaEventDestroy(e0); cudaEventDestroy(e1); return fail(h, LH_ECUDA, "autotune: z passes failed"); }
+    if (ms < best) { best = ms; best_tx = tx; }
+  }
+  h->tx = best_tx;
+  best = 1e30f;
+  for (int ch : {4, 8, 16, 32, 64}) {
+    h->chunk = ch;
+    const float ms = h->precision == LH_PREC_MIXED ? time_parts<float>(h, false, true, e0, e1)
+                                                   : time_parts<double>(h, false, true, e0, e1);
+    if (ms < 0.f) { h->chunk = ch0; cudaEventDestroy(e0); cudaEventDestroy(e1); return fail(h, LH_ECUDA, "autotune: product pass failed"); }
+    if (ms < best) { best = ms; best_ch = ch; }
+  }
+  h->chunk = best_ch;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CU(h, cudaGetLastError());
+  if (h->tx != tx0 || h->chunk != ch0) {  // the captured step carries the old launch shapes
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    ++h->graph_gen;
+  }
+  if (tx_out) *tx_out = h->tx;
+  if (chunk_out) *chunk_out = h->chunk;
   return LH_OK;
 }
 

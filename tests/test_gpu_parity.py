@@ -157,3 +157,20 @@ def test_conditional_statistics(oracle_mod):
         assert a.shape == b.shape, name
         tol = 1e-11 * np.abs(b).max() + 1e-13 * s.ngx * s.ngz
         assert np.abs(a - b).max() < tol, f"{name}: {np.abs(a - b).max():.3e} >= {tol:.3e}"
+
+
+def test_autotune_keeps_results(oracle_mod):
+    """Launch shapes change which CTA computes what, not the arithmetic: a tuned solver steps bit for bit
+    like an untuned one."""
+    o, s = _pair(oracle_mod, SMALL)
+    import littleharsh_gb300 as lh
+    t = lh.Solver(lh.Config(**SMALL))
+    t.set_fields(*s.get_fields())
+    tm = s.time()
+    t.set_time(0.0, tm["dt"], 0.0, tm["QxT"])
+    shapes = t.autotune()
+    assert shapes["tx"] in (1, 2, 4, 8, 16, 32) and shapes["chunk"] in (4, 8, 16, 32, 64)
+    s.step(3)
+    t.step(3)
+    for a, b in zip(t.get_fields(), s.get_fields()):
+        np.testing.assert_array_equal(a, b)
