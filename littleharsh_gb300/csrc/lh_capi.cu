@@ -310,7 +310,7 @@ int build_dt_tables(lh_handle* h) {
 
 // The plane work of the nonlinear term per band: which geometry and transforms
 // a band's planes use, and the centre and face levels it forms products on
-// (planelim, start.f90:1326-1378).
+// (planelim, start.f90:1336-1383).
 struct BandLaunch {
   const Dims* d;
   const FftPlan *pz, *ph, *pf;

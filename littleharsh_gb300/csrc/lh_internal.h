@@ -31,7 +31,7 @@ struct Dims {
                            // u levels Nu1+1..Nu2 and v levels Nv1+1..Nv2
 };
 
-// Long column test for stored mode (i, kk) (columns_long_list, start.f90:1100-1117).
+// Long column test for stored mode (i, kk) (columns_long_list, start.f90:1103-1117).
 __host__ __device__ inline bool is_long(const Dims& d, int i, int kk) {
   if (!d.banded) return true;
   const int kz = kk < d.snz / 2 ? kk : kk - d.snz;

@@ -161,13 +161,15 @@ class SRNet:
         new = lambda ch: torch.empty((Y, Z, X, ch), dtype=torch.bfloat16, device=x.device)  # noqa: E731
         h = new(CH)
         self._conv(0, x, h)
-        acts = [x, h]
+        acts = [x, h] if keep else None  # inference holds two activations at a time
         for b in range(self.nblocks):
             t = new(CH)
             self._conv(1 + 2 * b, h, t, flags=BIAS | RELU)
             h2 = new(CH)
             self._conv(2 + 2 * b, t, h2, res=h, flags=BIAS | RES)
-            acts += [t, h2]
+            if keep:
+                acts += [t, h2]
+            del t
             h = h2
         corr = torch.empty((Y, Z, X, COUT), dtype=torch.float32, device=x.device)
         self._conv(len(self.views) - 1, h, corr, out_f32=True)

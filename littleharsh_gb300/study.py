@@ -326,6 +326,8 @@ def main(argv=None):
     q.add_argument("--seed", type=int, default=1)
     q.add_argument("--max-steps", type=int, default=2_000_000)
     q.add_argument("--out", required=True)
+    r = sub.add_parser("warmstart-scale", help="the warm start's path on configuration 5's grids, timed")
+    r.add_argument("--out", required=True)
     a = ap.parse_args(argv)
     if a.cmd == "precision":
         res = precision_study(CONFIG1, re_tau=RE_TAU["config1"], spinup_turnovers=a.spinup_turnovers,
@@ -336,6 +338,12 @@ def main(argv=None):
         print(json.dumps({k: res[k] for k in ("grid", "steps", "t_end", "avg_turnovers", "l2_after_10_steps",
                                               "profile_err_vs_fp64", "max_profile_err", "fp64_twin_err_vs_fp64",
                                               "max_twin_err", "first_half", "gpu_ms_per_triple_step")}))
+    elif a.cmd == "warmstart-scale":
+        from . import warmstart
+        from .workloads import CONFIG5_COARSE, CONFIG5_FINE
+        res = warmstart.scale_check(CONFIG5_FINE, CONFIG5_COARSE, log=lambda m: print(m, flush=True))
+        with open(a.out, "w") as f:
+            json.dump(res, f)
     elif a.cmd == "warmstart":
         from . import warmstart
         from .workloads import CONFIG1_COARSE

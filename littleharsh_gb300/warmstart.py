@@ -446,3 +446,58 @@ def experiment(fine_cfg: dict, coarse_cfg: dict, re_tau: float, spinup_turnovers
     for s in sols:
         s.close()
     return res
+
+
+def scale_check(fine_cfg: dict, coarse_cfg: dict, coarse_steps: int = 20, fine_steps: int = 3, seed: int = 1,
+                cfl: float = 0.5, net=None, log=None) -> dict:
+    """The warm start's path at full size, timed: a coarse field (a few steps
+    from its seeded start), lifted onto the fine grid, corrected by the
+    network (an untrained one, whose correction is zero, unless `net` is
+    given), returned to spectral space, projected by the fine solver and
+    stepped.  Reports the time of each part and the divergence after the
+    projection."""
+    import torch
+    import littleharsh_gb300 as lh
+    from . import study
+    from .srnet import SRNet
+    out = {"fine": [fine_cfg["ngalx"], fine_cfg["ngalz"]], "coarse": [coarse_cfg["ngalx"], coarse_cfg["ngalz"]]}
+    c = lh.Solver(lh.Config(**coarse_cfg))
+    study.seeded_start([c], seed, cfl)
+    c.step(coarse_steps)
+    cgi = GridInfo(c)
+    cf = fields_to_device(c.get_fields()[:3])
+    c.close()
+    f = lh.Solver(lh.Config(**fine_cfg))
+    fgi = GridInfo(f)
+    out["fine_volume"] = [fgi.nyu, fgi.ngz, fgi.ngx]
+    net = net or SRNet(seed=seed)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lifted = lift(*cf, cgi, fgi)
+    base = to_volume(*lifted, fgi)
+    x = net_input(base, fgi)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    corr = net.forward(x)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    vol = base + getattr(net, "sigma", 1.0) * corr[..., :3]
+    u1, u2, u3 = [g.cpu().numpy() for g in from_volume(vol, fgi)]
+    del x, corr, base, vol, lifted
+    torch.cuda.empty_cache()
+    t3 = time.perf_counter()
+    f.set_fields(u1, u2, u3, np.zeros((f.nyp, f.nz, f.nkx), np.complex128))
+    f.project()
+    div = f.divmax()
+    t4 = time.perf_counter()
+    f.set_time(0.0, f.cfl_dt(cfl), 0.0)
+    f.step(fine_steps)
+    ms = f.last_step_ms()[0] / max(fine_steps, 1)
+    fields = f.get_fields()
+    out.update({"lift_s": t1 - t0, "network_s": t2 - t1, "to_spectral_s": t3 - t2, "project_s": t4 - t3,
+                "divmax_after_projection": div, "fine_ms_per_step": ms,
+                "finite_after_steps": bool(all(np.all(np.isfinite(a)) for a in fields))})
+    f.close()
+    if log:
+        log(str(out))
+    return out

@@ -395,7 +395,7 @@ struct lho {
 #define CIDX(s, jj, kk, ii) (2 * (((size_t)(jj) * (s)->nz + (kk)) * (s)->nkx + (ii)))
 
 /* Resolution of the physical plane of u level j / v level j: 0 wall bands, 1
- * middle band (planelim, start.f90:1326-1378). */
+ * middle band (planelim, start.f90:1336-1383). */
 static int res_u(const lho* s, int j) { return s->banded && j > s->N41 && j <= s->N42; }
 static int res_v(const lho* s, int j) { return s->banded && j > s->N31 && j <= s->N32; }
 
