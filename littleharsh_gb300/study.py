@@ -324,6 +324,7 @@ def main(argv=None):
     q.add_argument("--window", type=int, default=200)
     q.add_argument("--avg-windows", type=int, default=10)
     q.add_argument("--seed", type=int, default=1)
+    q.add_argument("--realisations", type=int, default=1)
     q.add_argument("--max-steps", type=int, default=2_000_000)
     q.add_argument("--out", required=True)
     r = sub.add_parser("warmstart-scale", help="the warm start's path on configuration 5's grids, timed")
@@ -350,10 +351,11 @@ def main(argv=None):
         res = warmstart.experiment(CONFIG1, CONFIG1_COARSE, RE_TAU["config1"], spinup_turnovers=a.spinup_turnovers,
                                    snapshots=a.snapshots, snap_every=a.snap_every, train_epochs=a.epochs,
                                    eval_turnovers=a.eval_turnovers, window=a.window, avg_windows=a.avg_windows,
-                                   seed=a.seed, max_steps=a.max_steps, log=lambda m: print(m, flush=True))
+                                   seed=a.seed, max_steps=a.max_steps, realisations=a.realisations,
+                                   log=lambda m: print(m, flush=True))
         with open(a.out, "w") as f:
             json.dump(res, f, default=float)
-        print(json.dumps({"starts": {k: v["stationary_step"] for k, v in res["starts"].items()},
+        print(json.dumps({"starts": {k: v["stationary_steps"] for k, v in res["starts"].items()},
                           "tol_effective": res["reference_run"]["tol_effective"],
                           "val": res["training"]["history"][-1]}))
 

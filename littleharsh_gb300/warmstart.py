@@ -324,18 +324,20 @@ def run_until(run, t_end: float, max_steps: int, on_window=None, log=None, tag="
 def experiment(fine_cfg: dict, coarse_cfg: dict, re_tau: float, spinup_turnovers: float = 15.0,
                snapshots: int = 200, snap_every: int = 100, train_epochs: int = 20, eval_turnovers: float = 15.0,
                window: int = 200, every: int = 10, avg_windows: int = 10, tol: float = 0.005, cfl: float = 0.5,
-               lr: float = 1e-3, seed: int = 1, max_steps: int = 2_000_000, log=None) -> dict:
+               lr: float = 1e-3, seed: int = 1, max_steps: int = 2_000_000, realisations: int = 1,
+               log=None) -> dict:
     """The learned warm start end to end on one fine/coarse grid pair.
 
     1. fine run from the seeded laminar + noise start: spin-up, then the
        converged statistics and `snapshots` snapshots `snap_every` steps apart;
     2. coarse run from its own seeded start to a stationary field;
     3. pairs from the snapshots (last 10% held out), network training;
-    4. three fine runs advanced together from: a fresh laminar + noise field,
-       the lifted coarse field, and the lifted field corrected by the network
-       (the last two projected divergence free); steps until each run's
-       statistics stay within `tol` (or the noise floor of the converged
-       statistics, if larger) of the converged ones.
+    4. fine runs advanced together from: a fresh laminar + noise field, the
+       lifted coarse field, and the lifted field corrected by the network (the
+       last two projected divergence free), `realisations` of each (their own
+       seeds and coarse runs); steps until each run's statistics stay within
+       `tol` (or the noise floor of the converged statistics, if larger) of
+       the converged ones.
     """
     import littleharsh_gb300 as lh
     from . import study
@@ -397,17 +399,19 @@ def experiment(fine_cfg: dict, coarse_cfg: dict, re_tau: float, spinup_turnovers
     run.close()
     fine.close()
 
-    # 2. coarse run to a stationary field
-    coarse = lh.Solver(lh.Config(**coarse_cfg))
-    study.seeded_start([coarse], seed + 1, cfl)
-    crun = study.LongRun([coarse], cfl=cfl, window=window, every=every)
+    # 2. coarse runs (one per realisation) to stationary fields, advanced together
+    coarses = [lh.Solver(lh.Config(**coarse_cfg)) for _ in range(realisations)]
+    for q, c in enumerate(coarses):
+        study.seeded_start([c], seed + 1 + 10 * q, cfl)
+    crun = study.LongRun(coarses, cfl=cfl, window=window, every=every)
     run_until(crun, t_spin, max_steps, log=log, tag="coarse")
-    cf = fields_to_device(coarse.get_fields()[:3])
-    res["coarse_run"] = {"steps": crun.steps, "t": coarse.time()["t"],
+    cfs = [fields_to_device(c.get_fields()[:3]) for c in coarses]
+    res["coarse_run"] = {"steps": crun.steps, "t": coarses[0].time()["t"],
                          "series": [{"step": r["step"], "t": r["t"], "mpgx": r["mpgx"], "tke": r["tke"]}
                                     for r in crun.records[0]]}
     crun.close()
-    coarse.close()
+    for c in coarses:
+        c.close()
 
     # 3. training
     nval = max(1, len(pairs) // 10)
@@ -419,32 +423,46 @@ def experiment(fine_cfg: dict, coarse_cfg: dict, re_tau: float, spinup_turnovers
                        "seconds": time.perf_counter() - t_tr, "history": hist,
                        "params": int(sum(27 * ci * co + co for ci, co in net.shapes))}
 
-    # 4. the three starts
-    starts = {}
-    sols = [lh.Solver(lh.Config(**fine_cfg)) for _ in range(3)]
-    study.seeded_start([sols[0]], seed + 2, cfl)
-    for s, use_net in ((sols[1], False), (sols[2], True)):
-        u1, u2, u3 = warm_field(net, *cf, coarse_gi, fgi, use_net=use_net)
-        s.set_fields(u1, u2, u3, np.zeros((s.nyp, s.nz, s.nkx), np.complex128))
-        s.project()
-        s.set_time(0.0, s.cfl_dt(cfl), ref_mpgx, qxt)
-    for s in sols:
-        tm = s.time()
-        s.set_time(0.0, min(x.cfl_dt(cfl) for x in sols), tm["mpgx"], qxt)
+    # 4. the three starts, `realisations` of each, advanced together in one ensemble
+    names = ("laminar_noise", "lifted", "lifted_net")
+    sols, kinds = [], []
+    for q in range(realisations):
+        for kind in names:
+            s_ = lh.Solver(lh.Config(**fine_cfg))
+            if kind == "laminar_noise":
+                study.seeded_start([s_], seed + 2 + 10 * q, cfl)
+            else:
+                u1, u2, u3 = warm_field(net, *cfs[q], coarse_gi, fgi, use_net=(kind == "lifted_net"))
+                s_.set_fields(u1, u2, u3, np.zeros((s_.nyp, s_.nz, s_.nkx), np.complex128))
+                s_.project()
+                s_.set_time(0.0, s_.cfl_dt(cfl), ref_mpgx, qxt)
+            sols.append(s_)
+            kinds.append(kind)
+    dt_common = min(x.cfl_dt(cfl) for x in sols)
+    for s_ in sols:
+        tm = s_.time()
+        s_.set_time(0.0, dt_common, tm["mpgx"], qxt)
     erun = study.LongRun(sols, cfl=cfl, window=window, every=every)
     run_until(erun, eval_turnovers * T, max_steps, log=log, tag="starts")
-    for i, name in enumerate(("laminar_noise", "lifted", "lifted_net")):
+    starts = {k: {"runs": []} for k in names}
+    for i, kind in enumerate(kinds):
         rr = erun.records[i]
         devs = study.deviation_series(rr, ref_prof, ref_mpgx, sols[i].ngx, sols[i].ngz, erun.grids, avg_windows)
-        starts[name] = {"stationary_step": study.stationary_from(rr, devs, tol_eff, avg_windows),
-                        "first_dev": devs[avg_windows - 1] if len(devs) >= avg_windows else None,
-                        "series": [{"step": r["step"], "t": r["t"], "mpgx": r["mpgx"], "tke": r["tke"], "dev": d}
-                                   for r, d in zip(rr, devs)]}
+        starts[kind]["runs"].append({"stationary_step": study.stationary_from(rr, devs, tol_eff, avg_windows),
+                                     "first_dev": devs[avg_windows - 1] if len(devs) >= avg_windows else None,
+                                     "series": [{"step": r["step"], "t": r["t"], "mpgx": r["mpgx"], "tke": r["tke"],
+                                                 "dev": d} for r, d in zip(rr, devs)]})
+    for kind in names:
+        st = [r["stationary_step"] for r in starts[kind]["runs"]]
+        ok = [x for x in st if x is not None]
+        starts[kind]["stationary_steps"] = st
+        starts[kind]["mean_stationary_step"] = float(np.mean(ok)) if len(ok) == len(st) and ok else None
     res["starts"] = starts
     res["eval_steps"] = erun.steps
+    res["dt_common_start"] = dt_common
     erun.close()
-    for s in sols:
-        s.close()
+    for s_ in sols:
+        s_.close()
     return res
 
 

@@ -174,3 +174,35 @@ def test_autotune_keeps_results(oracle_mod):
     t.step(3)
     for a, b in zip(t.get_fields(), s.get_fields()):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("cfg", [SMALL, C1], ids=["canopy24", "config1_96x97"])
+def test_broadband_field(oracle_mod, cfg):
+    """Every mode populated (not only |k| <= 8): the high modes, the 3/2 truncation and the Nyquist
+    neighbours are exercised as in developed turbulence.  FP64 to the usual bar; the mixed form to
+    FP32 accuracy."""
+    import littleharsh_gb300 as lh
+    from littleharsh_gb300.initial import initial_field
+    o = oracle_mod.Oracle(**cfg)
+    g = o.grid()
+    kmax = max(o.nkx, o.nz)
+    o.set_fields(*initial_field(g["yu"], g["yv"], o.nz, o.nkx, o.nyp, seed=7, amp=0.2, kmax=kmax))
+    o.set_scalars(0.0, 1.0, 0.0)
+    o.project()
+    u1, u2, u3, p = o.get_fields()
+    dt, Q = o.cfl_dt(0.5), o.flowrate()
+    o.set_scalars(0.0, dt, 0.0, Q)
+    sols = []
+    for prec in (lh.PREC_FP64, lh.PREC_MIXED):
+        s = lh.Solver(lh.Config(**cfg), precision=prec)
+        s.set_fields(u1, u2, u3, p)
+        s.set_time(0.0, dt, 0.0, Q)
+        sols.append(s)
+    o.step(3)
+    for s in sols:
+        s.step(3)
+    ref = o.get_fields()
+    for name, a, b in zip(("u1", "u2", "u3", "p"), sols[0].get_fields(), ref):
+        assert rel_l2(a, b) < 1e-11, f"fp64 {name}: {rel_l2(a, b):.3e}"
+    errs = [rel_l2(a, b) for a, b in zip(sols[1].get_fields(), ref)]
+    assert max(errs[:3]) < 2e-6 and errs[3] < 1e-4, f"mixed: {errs}"
