@@ -178,6 +178,20 @@ def grid_points(cfg: dict, nyu: int, N) -> int:
     return fine * (nyu - nmid) + coarse * nmid
 
 
+def band_geometry(cfg: dict, s):
+    """(ngx, ngz, nkx, nz, centres, faces) of the plane work of each band: one
+    entry without variable resolution; the wall bands' and the middle band's
+    with it (middle band: u centres N(4,1)+1..N(4,2), v faces N(3,1)+1..N(3,2))."""
+    nl_u, nl_v = s.nyu - 2, s.nyv - 2
+    if not cfg.get("ngalx2") and not cfg.get("ngalz2"):
+        return [(s.ngx, s.ngz, s.nkx, s.nz, nl_u, nl_v)]
+    N = list(s.params.N)
+    mid_u, mid_v = N[2 * 4 + 3] - N[1 * 4 + 3], N[2 * 4 + 2] - N[1 * 4 + 2]
+    gx2, gz2 = cfg.get("ngalx2") or cfg["ngalx"], cfg.get("ngalz2") or cfg["ngalz"]
+    return [(s.ngx, s.ngz, s.nkx, s.nz, nl_u - mid_u, nl_v - mid_v),
+            (gx2, gz2, (2 * (gx2 // 3)) // 2 + 1, 2 * (gz2 // 3), mid_u, mid_v)]
+
+
 def max_over_ranks(value: float, dist, device: str) -> float:
     """The slowest rank's timing (replicas only: no data moves between ranks)."""
     if dist is None:
@@ -322,20 +336,25 @@ def run_ours(args, rank: int, world: int, local_rank: int, dist):
         dom = max(prof, key=lambda k: prof[k][0])
         dms, dn = prof[dom]
         per_launch_ms = dms / max(dn, 1)
-        d = {"ngx": s.ngx, "ngz": s.ngz, "nkx": s.nkx, "nz": s.nz, "nyu": s.nyu, "nyv": s.nyv}
-        nl_u, nl_v = s.nyu - 2, s.nyv - 2
-        mp, npl = s.nkx * s.ngz, s.nkx * s.nz
         csz = 16 if prec == lh.PREC_FP64 else 8
-        # compulsory bytes and model FLOPs per launch of each pipeline kernel
-        model = {
-            "zinv": ((2 * nl_u + nl_v) * (npl * 16 + mp * csz), z_flops(s.ngz, s.nkx, 2 * nl_u + nl_v)),
-            "xprod": ((2 * nl_u + nl_v + 4 * nl_u + 2 * nl_v) * mp * csz, xprod_flops(s.ngx, s.ngz, s.nkx, nl_u)),
-            "zfwd": ((4 * nl_u + 2 * nl_v) * (mp * csz + npl * 16),
-                     z_flops(s.ngz, s.nkx, 4 * nl_u + 2 * nl_v, prune_last=(s.ngz % 3 == 0 and s.nz * 3 == 2 * s.ngz))),
-            "assemble": (19 * s.nyu * npl * 16, 0.0),
-            "vsolve": (4 * (2 * s.nyu + s.nyv) * npl * 16, 0.0),
-            "psolve": ((16 + 16 + 16 + 8 + 8) * s.nyp * npl + 14 * 16 * s.nyp * npl, 0.0),
-        }
+        npl = s.nkx * s.nz
+        # compulsory bytes and model FLOPs per step of each pipeline kernel, summed over the bands' planes
+        # (one band without variable resolution), then divided by the kernel's launches per step
+        model_step = {"zinv": [0, 0.0], "xprod": [0, 0.0], "zfwd": [0, 0.0]}
+        for (gx, gz, kx, kz, nc, nf) in band_geometry(cfg, s):
+            mpb = kx * gz
+            prune = gz % 3 == 0 and kz * 3 == 2 * gz
+            model_step["zinv"][0] += 3 * (2 * nc + nf) * (kx * kz * 16 + mpb * csz)
+            model_step["zinv"][1] += 3 * z_flops(gz, kx, 2 * nc + nf)
+            model_step["xprod"][0] += 3 * (2 * nc + nf + 4 * nc + 2 * nf) * mpb * csz
+            model_step["xprod"][1] += 3 * xprod_flops(gx, gz, kx, nc)
+            model_step["zfwd"][0] += 3 * (4 * nc + 2 * nf) * (mpb * csz + kx * kz * 16)
+            model_step["zfwd"][1] += 3 * z_flops(gz, kx, 4 * nc + 2 * nf, prune_last=prune)
+        model_step["assemble"] = [3 * 19 * s.nyu * npl * 16, 0.0]
+        model_step["vsolve"] = [3 * 4 * (2 * s.nyu + s.nyv) * npl * 16, 0.0]
+        model_step["psolve"] = [3 * ((16 + 16 + 16 + 8 + 8) * s.nyp * npl + 14 * 16 * s.nyp * npl), 0.0]
+        model = {k: (v[0] / max(prof.get(k, (0.0, 1))[1], 1), v[1] / max(prof.get(k, (0.0, 1))[1], 1))
+                 for k, v in model_step.items()}
         bytes_l, flops_l = model.get(dom, (0, 0.0))
         ach_gbs = bytes_l / (per_launch_ms * 1e-3) / 1e9 if bytes_l else None
         traffic = None

@@ -482,7 +482,8 @@ int substage(lh_handle* h, int k, int upto) {
 }
 
 int count_launches(const lh_handle* h) {
-  int per = 6 + (h->prm.flag_ctpress == 0 ? 1 : 0);  // zinv, xprod, zfwd, assemble, vsolve, psolve (+flowrate)
+  // zinv, xprod, zfwd per band; assemble, vsolve, psolve (+flowrate)
+  int per = 3 * (h->d.banded ? 3 : 1) + 3 + (h->prm.flag_ctpress == 0 ? 1 : 0);
   if (h->nibu + h->nibv > 0) per += 3;
   return 3 * per;
 }
