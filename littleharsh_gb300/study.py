@@ -327,6 +327,12 @@ def main(argv=None):
     q.add_argument("--realisations", type=int, default=1)
     q.add_argument("--max-steps", type=int, default=2_000_000)
     q.add_argument("--out", required=True)
+    e = sub.add_parser("precision-ensemble", help="several FP64 and mixed realisations on configuration 1's grid")
+    e.add_argument("--realisations", type=int, default=3)
+    e.add_argument("--spinup-turnovers", type=float, default=3.0)
+    e.add_argument("--avg-turnovers", type=float, default=15.0)
+    e.add_argument("--max-seconds", type=float, default=1e30)
+    e.add_argument("--out", required=True)
     r = sub.add_parser("warmstart-scale", help="the warm start's path on configuration 5's grids, timed")
     r.add_argument("--out", required=True)
     a = ap.parse_args(argv)
@@ -339,6 +345,14 @@ def main(argv=None):
         print(json.dumps({k: res[k] for k in ("grid", "steps", "t_end", "avg_turnovers", "l2_after_10_steps",
                                               "profile_err_vs_fp64", "max_profile_err", "fp64_twin_err_vs_fp64",
                                               "max_twin_err", "first_half", "gpu_ms_per_triple_step")}))
+    elif a.cmd == "precision-ensemble":
+        res = precision_ensemble(CONFIG1, realisations=a.realisations, re_tau=RE_TAU["config1"],
+                                 spinup_turnovers=a.spinup_turnovers, avg_turnovers=a.avg_turnovers,
+                                 max_seconds=a.max_seconds, log=lambda m: print(m, flush=True))
+        with open(a.out, "w") as f:
+            json.dump(res, f)
+        print(json.dumps({k: res[k] for k in ("realisations", "steps", "avg_turnovers", "mean_profile_err_mixed_vs_fp64",
+                                              "fp64_mean_standard_error", "tke_fp64", "tke_mixed")}))
     elif a.cmd == "warmstart-scale":
         from . import warmstart
         from .workloads import CONFIG5_COARSE, CONFIG5_FINE
@@ -415,3 +429,61 @@ def stationary_from(records, devs, tol: float, avg: int, hold: int | None = None
         return None
     first = ok_from - avg + 1
     return records[first - 1]["step"] if first > 0 else 0
+
+
+def precision_ensemble(cfg: dict, realisations: int = 3, re_tau: float = 180.0, spinup_turnovers: float = 3.0,
+                       avg_turnovers: float = 15.0, window: int = 400, every: int = 10, seed: int = 11,
+                       cfl: float = 0.5, max_steps: int = 400000, max_seconds: float = 1e30, log=None) -> dict:
+    """FP64 and mixed runs from `realisations` seeded fields (one FP64 and one
+    mixed run per field), all in one ensemble graph with a common dt.  The
+    mean profiles of the FP64 runs are compared with those of the mixed runs;
+    the spread of the FP64 runs' own profiles (standard error of their mean)
+    is the sampling noise of that comparison."""
+    import littleharsh_gb300 as lh
+    sols = []
+    for q in range(realisations):
+        fp = lh.Solver(lh.Config(**cfg), precision=lh.PREC_FP64)
+        mx = lh.Solver(lh.Config(**cfg), precision=lh.PREC_MIXED)
+        seeded_start([fp, mx], seed + q, cfl)
+        sols += [fp, mx]
+    dt = min(s.cfl_dt(cfl) for s in sols)
+    for s in sols:
+        s.set_time(0.0, dt, 0.0)
+    run = LongRun(sols, cfl=cfl, window=window, every=every)
+    T = cfg["Re"] / re_tau
+    t_spin, t_end = spinup_turnovers * T, (spinup_turnovers + avg_turnovers) * T
+    w0 = time.perf_counter()
+    while sols[0].time()["t"] < t_end and run.steps < max_steps and time.perf_counter() - w0 < max_seconds:
+        run.advance_window()
+        if log and len(run.records[0]) % 25 == 0:
+            log(f"step {run.steps} t {sols[0].time()['t']:.1f} tke " +
+                " ".join(f"{run.records[i][-1]['tke']:.4f}" for i in range(len(sols))) +
+                f" ({time.perf_counter() - w0:.0f} s)")
+    masks = interior(run.grids)
+    profs = [run.average(i, t_spin) for i in range(len(sols))]
+    fp_p, mx_p = profs[0::2], profs[1::2]
+    mean = lambda ps: {k: np.mean([p[k] for p in ps], axis=0) for k in PROFILE_KEYS}  # noqa: E731
+    fpm, mxm = mean(fp_p), mean(mx_p)
+    err = profile_errors(mxm, fpm, masks)
+    # standard error of the FP64 mean, per profile, relative to the profile's maximum
+    sem = {}
+    for k in PROFILE_KEYS:
+        m = masks[_GRID[k][0]]
+        arr = np.array([p[k][m] for p in fp_p])
+        sd = arr.std(axis=0, ddof=1) if len(fp_p) > 1 else np.zeros(arr.shape[1])
+        sem[k] = float(np.max(sd) / np.sqrt(len(fp_p)) / np.max(np.abs(fpm[k][m])))
+    tke_avg = []
+    for i in range(len(sols)):
+        rr = [r for r in run.records[i] if r["t"] >= t_spin]
+        tke_avg.append(float(np.mean([r["tke"] for r in rr])) if rr else None)
+    res = {"grid": [sols[0].ngx, sols[0].ngz, sols[0].nyu], "realisations": realisations, "seeds": [seed + q for q in range(realisations)],
+           "steps": run.steps, "t_end": sols[0].time()["t"], "avg_turnovers": (sols[0].time()["t"] - t_spin) / T,
+           "mean_profile_err_mixed_vs_fp64": err, "max_mean_profile_err": max(err.values()),
+           "fp64_mean_standard_error": sem, "tke_fp64": tke_avg[0::2], "tke_mixed": tke_avg[1::2],
+           "gpu_ms_per_ensemble_step": run.gpu_ms / max(run.steps, 1),
+           "profiles": {"y_u": run.grids["u"].tolist(), "fp64_mean": {k: v.tolist() for k, v in fpm.items()},
+                        "mixed_mean": {k: v.tolist() for k, v in mxm.items()}}}
+    run.close()
+    for s in sols:
+        s.close()
+    return res
