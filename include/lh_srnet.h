@@ -41,6 +41,18 @@ int lh_sr_conv_fwd(int32_t cin, int32_t cout, const void* in, const void* w, con
                    int32_t out_f32, const void* res, const void* gate, int32_t flags, int32_t X, int32_t Y, int32_t Z,
                    void* stream);
 
+/* The same convolution on the tcgen05 tensor cores (TMEM accumulator, one
+ * elected thread issuing the MMAs, an mbarrier per tile); Z must also be a
+ * multiple of 4.  A tile whose MMAs do not complete within a bounded wait is
+ * skipped and recorded for lh_sr_tc_status. */
+int lh_sr_conv_fwd_tc(int32_t cin, int32_t cout, const void* in, const void* w, const float* bias, void* out,
+                      int32_t out_f32, const void* res, const void* gate, int32_t flags, int32_t X, int32_t Y,
+                      int32_t Z, void* stream);
+
+/* Synchronous: *timed_out = 1 if a tcgen05 convolution gave up waiting since
+ * the last call (and clears the record). */
+int lh_sr_tc_status(int32_t* timed_out);
+
 /* dw[tap][co][ci] += sum_v dout[v][co] * in[v + offset(tap)][ci]; db[co] += sum_v dout[v][co].
  * dw, db fp32 (accumulated into: zero them first). */
 int lh_sr_conv_wgrad(int32_t cin, int32_t cout, const void* in, const void* dout, float* dw, float* db, int32_t X,

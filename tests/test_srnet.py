@@ -232,3 +232,35 @@ def test_network_gradient_matches_oracle():
         assert err < 5e-2 and cos > 0.998, (ci, co, err, cos)
         errb = np.linalg.norm(got_b - gb) / max(np.linalg.norm(gb), 1e-30)
         assert errb < 5e-2, (ci, co, errb)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cin,cout,f32", [(16, 32, False), (32, 32, False), (32, 16, False), (32, 16, True)])
+@pytest.mark.parametrize("flags", [so.BIAS | so.RELU, so.GATE | so.RES])
+def test_conv_fwd_tcgen05(lib, cin, cout, f32, flags):
+    """The tcgen05 (TMEM accumulator) form of the forward convolution against the oracle."""
+    import ctypes
+    import torch
+    from littleharsh_gb300 import srnet
+    rng = np.random.default_rng(500 + cin * 10 + cout + flags)
+    Y, Z, X = VOL
+    x = so.bf16_round(rng.standard_normal((Y, Z, X, cin)))
+    w = so.bf16_round(rng.standard_normal((27, cout, cin)) / np.sqrt(27 * cin))
+    b = rng.standard_normal(cout).astype(np.float32)
+    res = so.bf16_round(rng.standard_normal((Y, Z, X, cout)))
+    gate = so.bf16_round(rng.standard_normal((Y, Z, X, cout)))
+    ref = so.conv_fwd(x, w, b, res, gate, flags)
+    out = torch.empty((Y, Z, X, cout), dtype=torch.float32 if f32 else torch.bfloat16, device="cuda")
+    xt, wt, bt, rt, gt = _t(x, torch.bfloat16), _t(w, torch.bfloat16), _t(b, torch.float32), \
+        _t(res, torch.bfloat16), _t(gate, torch.bfloat16)
+    rc = lib.lh_sr_conv_fwd_tc(cin, cout, srnet._ptr(xt), srnet._ptr(wt), srnet._ptr(bt), srnet._ptr(out), int(f32),
+                               srnet._ptr(rt), srnet._ptr(gt), flags, X, Y, Z, None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    timed_out = ctypes.c_int32(-1)
+    assert lib.lh_sr_tc_status(ctypes.byref(timed_out)) == 0 and timed_out.value == 0
+    got = out.float().cpu().numpy()
+    if f32:
+        np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5)
+    else:
+        np.testing.assert_allclose(got, ref, rtol=2 ** -8, atol=1e-3)
