@@ -438,7 +438,9 @@ def run_srnet(args):
     peaks = _peaks()
     net = SRNet(seed=0)
     out = {"metric": "SR network bf16 TFLOP/s", "unit": "TFLOP/s", "higher_is_better": True, "n_gpus": 1,
-           "dtype": "bf16 (fp32 accumulate)", "kernel": "mma.sync m16n8k16 implicit-GEMM 3x3x3 conv"}
+           "dtype": "bf16 (fp32 accumulate)",
+           "kernel": "3x3x3 implicit-GEMM conv: forward and data gradient on tcgen05 (TMEM accumulator); weight "
+                     "gradient on mma.sync m16n8k16; the mma.sync forward timed beside it"}
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
     cases = [("train_step_config1", CONFIG1, True), ("inference_config5_fine", CONFIG5_FINE, False)]
     if args.sr_small:  # profiler captures: the configuration-1 training step only
@@ -460,21 +462,26 @@ def run_srnet(args):
                 net.adam_step()
             else:
                 net.forward(x)
-        for _ in range(max(args.warmup, 1)):
-            step()
-        torch.cuda.synchronize()
-        a, b = ev(), ev()
-        n = max(args.steps, 1)
-        a.record()
-        for _ in range(n):
-            step()
-        b.record()
-        torch.cuda.synchronize()
-        ms = a.elapsed_time(b) / n
+        res = {}
+        for tc in (True, False):
+            net.tcgen05 = tc
+            for _ in range(max(args.warmup, 1)):
+                step()
+            torch.cuda.synchronize()
+            a, b = ev(), ev()
+            n = max(args.steps, 1)
+            a.record()
+            for _ in range(n):
+                step()
+            b.record()
+            torch.cuda.synchronize()
+            res[tc] = a.elapsed_time(b) / n
         fl = srnet_flops(Y, Z, X, train)
-        tf = fl / (ms * 1e-3) / 1e12
-        out[name] = {"volume": [Y, Z, X], "ms": ms, "tflops": tf, "flops": fl,
-                     "frac_of_bf16_peak": tf / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None}
+        tf = fl / (res[True] * 1e-3) / 1e12
+        out[name] = {"volume": [Y, Z, X], "ms": res[True], "tflops": tf, "flops": fl,
+                     "frac_of_bf16_peak": tf / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None,
+                     "ms_mma_sync_forward": res[False], "tflops_mma_sync_forward": fl / (res[False] * 1e-3) / 1e12}
+        net.tcgen05 = True
         del x, base, tgt
         torch.cuda.empty_cache()
     out["value"] = out["train_step_config1"]["tflops"]

@@ -75,7 +75,7 @@ class SRNet:
     """Parameters, activations and the training step on the current CUDA device."""
 
     def __init__(self, params=None, seed: int = 0, nblocks: int = NBLOCKS, lr: float = 1e-3,
-                 betas=(0.9, 0.999), eps: float = 1e-8, weight_decay: float = 0.0):
+                 betas=(0.9, 0.999), eps: float = 1e-8, weight_decay: float = 0.0, tcgen05: bool = True):
         torch = _torch()
         self.nblocks = nblocks
         self.shapes = layer_shapes(nblocks)
@@ -106,6 +106,7 @@ class SRNet:
         self.flip = [torch.zeros(27 * vw["ci"] * vw["co"], dtype=torch.bfloat16, device=dev) for vw in self.views]
         self.lr, self.betas, self.eps, self.wd = lr, betas, eps, weight_decay
         self.t = 0
+        self.tcgen05 = tcgen05  # forward and data-gradient convolutions on tcgen05 (else mma.sync)
         self.sigma = 1.0  # scale of the correction (set by training: rms of the residual it learns)
         self._acts = None
         self._shape = None
@@ -135,8 +136,9 @@ class SRNet:
         co = cout if cout is not None else vw["co"]
         w = weights if weights is not None else vw["w"]
         Y, Z, X = self._shape
-        _check(L.lh_sr_conv_fwd(ci, co, _ptr(x), _ptr(w), _ptr(vw["b"]) if flags & BIAS else None, _ptr(out),
-                                int(out_f32), _ptr(res), _ptr(gate), flags, X, Y, Z, _stream()), "lh_sr_conv_fwd")
+        fn = L.lh_sr_conv_fwd_tc if (self.tcgen05 and Z % 4 == 0) else L.lh_sr_conv_fwd
+        _check(fn(ci, co, _ptr(x), _ptr(w), _ptr(vw["b"]) if flags & BIAS else None, _ptr(out),
+                  int(out_f32), _ptr(res), _ptr(gate), flags, X, Y, Z, _stream()), "lh_sr_conv_fwd")
 
     def _wgrad(self, li, x, dout):
         L = load_library()
