@@ -412,6 +412,16 @@ def deviation_series(records, ref_prof, ref_mpgx, ngx, ngz, grids, avg: int) -> 
     return out
 
 
+def first_within(records, devs, tol: float, avg: int):
+    """First step at which a block of `avg` windows comes within tol of the
+    reference statistics (the step at which that block begins), or None."""
+    for w in range(avg - 1, len(devs)):
+        if devs[w] <= tol:
+            first = w - avg + 1
+            return records[first - 1]["step"] if first > 0 else 0
+    return None
+
+
 def stationary_from(records, devs, tol: float, avg: int, hold: int | None = None):
     """First step from which every later block of `avg` windows stays within
     tol of the reference statistics (the step at which the first such block

@@ -449,6 +449,7 @@ def experiment(fine_cfg: dict, coarse_cfg: dict, re_tau: float, spinup_turnovers
         rr = erun.records[i]
         devs = study.deviation_series(rr, ref_prof, ref_mpgx, sols[i].ngx, sols[i].ngz, erun.grids, avg_windows)
         starts[kind]["runs"].append({"stationary_step": study.stationary_from(rr, devs, tol_eff, avg_windows),
+                                     "first_within_step": study.first_within(rr, devs, tol_eff, avg_windows),
                                      "first_dev": devs[avg_windows - 1] if len(devs) >= avg_windows else None,
                                      "series": [{"step": r["step"], "t": r["t"], "mpgx": r["mpgx"], "tke": r["tke"],
                                                  "dev": d} for r, d in zip(rr, devs)]})
@@ -456,6 +457,7 @@ def experiment(fine_cfg: dict, coarse_cfg: dict, re_tau: float, spinup_turnovers
         st = [r["stationary_step"] for r in starts[kind]["runs"]]
         ok = [x for x in st if x is not None]
         starts[kind]["stationary_steps"] = st
+        starts[kind]["first_within_steps"] = [r["first_within_step"] for r in starts[kind]["runs"]]
         starts[kind]["mean_stationary_step"] = float(np.mean(ok)) if len(ok) == len(st) and ok else None
     res["starts"] = starts
     res["eval_steps"] = erun.steps
