@@ -360,20 +360,28 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
 
 // ---- tcgen05 forward convolution ------------------------------------------------
 //
-// The same convolution on the 5th-generation tensor cores: one elected thread
-// issues tcgen05.mma (M = 128 voxels, N = Cout, K = 16 channels of one tap,
-// bf16 operands from shared memory, fp32 accumulator in TMEM), 27 x Cin/16 of
-// them per tile, completion signalled on an mbarrier; four warps then read the
-// accumulator rows back with tcgen05.ld for the epilogue.  A tile is 4 z-rows x
-// 32 x-voxels of one y level.  Operands use the no-swizzle K-major layout
-// (core matrices of 8 rows x 16 bytes; rows 16 bytes apart): the A operand of a
-// tap is 128 consecutive rows of a staged halo copy, so each of the three x
-// shifts gets its own copy ([kchunk][dy][z row][x], z rows exactly 32 rows
-// apart) and a tap is a start address.  Weights are [tap][kchunk][cout] rows.
-constexpr int TC_TZ = 4;
-constexpr int TC_ZR = TC_TZ + 2;            // staged z rows
-constexpr int TC_ROWS = 3 * TC_ZR * TX;     // rows of one x-shifted copy (dy, z row, x)
-constexpr unsigned kTcSpinLimit = 1u << 20; // bound of every mbarrier wait
+// The same convolution on the 5th-generation tensor cores.  A tile is 8 z-rows
+// x 32 x-voxels of one y level (M = 256 as two M = 128 halves, two fp32
+// accumulators of Cout columns in TMEM).  Its work runs as three stages, one
+// per y offset dy of the taps: a stage stages the dy level's halo (10 z-rows x
+// 32 voxels for each of the three x shifts, so that the A operand of a tap is
+// 128 consecutive rows, i.e. a start address) into one of two shared-memory
+// buffers, then one elected thread issues the stage's 9 taps x Cin/16 x 2
+// tcgen05.mma (K = 16 channels, bf16 operands from shared memory) and commits
+// them to the buffer's mbarrier.  While the tensor cores work on stage s, all
+// threads stage s + 1 into the other buffer (after that buffer's previous MMAs
+// completed), so staging and MMAs overlap across stages and tiles.  After a
+// tile's last stage eight warps read the accumulators back with tcgen05.ld
+// (warp w: TMEM lanes 32 (w mod 4), half w / 4) for the epilogue.
+// Operands use the no-swizzle K-major layout (core matrices of 8 rows x 16
+// bytes, rows 16 bytes apart): A rows [x shift][k chunk][z row][x] with the
+// k-chunk planes padded by 2 rows against bank conflicts; weights rows
+// [tap][k chunk][cout].  Every mbarrier wait is bounded.
+constexpr int TC_TZ = 8;                     // z rows per tile
+constexpr int TC_ZR = TC_TZ + 2;             // staged z rows per dy
+constexpr int TC_PLANE = TC_ZR * TX + 2;     // 16-byte rows per k-chunk plane (2 rows of padding)
+constexpr int TC_THREADS = 256;
+constexpr unsigned kTcSpinLimit = 1u << 20;  // bound of every mbarrier wait
 
 __device__ __forceinline__ uint64_t tc_smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
   // start address, leading (K) and stride (M/N) byte offsets in 16-byte units, descriptor version 1,
@@ -387,33 +395,48 @@ __host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
+// bounded wait for the phase of parity `parity` of an mbarrier; false if it ran out
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done = 0;
+  for (unsigned it = 0; it < kTcSpinLimit && !done; ++it) {
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity));
+  }
+  return done != 0;
+}
+
 template <int CIN, int COUT, typename OutT>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(TC_THREADS, 1)
     k_conv_fwd_tc(const __nv_bfloat16* __restrict__ in, const __nv_bfloat16* __restrict__ w,
                   const float* __restrict__ bias, OutT* __restrict__ out, const __nv_bfloat16* __restrict__ res,
                   const __nv_bfloat16* __restrict__ gate, int epi, Vol v, int* __restrict__ err) {
-  constexpr int KC = CIN / 8;                       // 16-byte chunks (core-matrix columns) per row
-  constexpr uint32_t A_LBO = TC_ROWS * 16;          // next K chunk of a copy
-  constexpr uint32_t B_LBO = COUT * 16;             // next K chunk of a tap's weights
-  constexpr size_t A_COPY = (size_t)KC * TC_ROWS;   // 16-byte rows per copy
+  constexpr int KC = CIN / 8;                       // 16-byte chunks (core-matrix columns) per voxel row
+  constexpr int LKC = KC == 4 ? 2 : 1;              // log2 KC (CIN = 32 or 16)
+  constexpr uint32_t A_LBO = TC_PLANE * 16;         // next k chunk of an x-shift copy
+  constexpr uint32_t B_LBO = COUT * 16;             // next k chunk of a tap's weights
+  constexpr int A_SHIFT = KC * TC_PLANE;            // 16-byte rows per x-shift copy
+  constexpr int A_BUF = 3 * A_SHIFT;                // rows per stage buffer
+  constexpr int UNITS = 3 * TC_ZR * TX;             // voxel rows staged per stage
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint4* sA = reinterpret_cast<uint4*>(smem_raw);                // [3 dx][KC][TC_ROWS]
-  uint4* sB = sA + 3 * A_COPY;                                   // [27][KC][COUT]
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sB + (size_t)27 * KC * COUT);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+  uint4* sA = reinterpret_cast<uint4*>(smem_raw);   // [2 buffers][3 dx][KC][TC_PLANE]
+  uint4* sB = sA + 2 * A_BUF;                       // [27][KC][COUT]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sB + (size_t)27 * KC * COUT);  // one per buffer
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-  // weights [27][COUT][CIN] -> [27][KC][COUT] 16-byte rows
-  for (int c = threadIdx.x; c < 27 * COUT * KC; c += blockDim.x) {
+  for (int c = threadIdx.x; c < 27 * COUT * KC; c += blockDim.x) {  // weights -> [27][KC][COUT] rows
     const int kc = c % KC, n = (c / KC) % COUT, tap = c / (KC * COUT);
     cp_async16(sB + ((size_t)tap * KC + kc) * COUT + n, w + ((size_t)tap * COUT + n) * CIN + kc * 8, true);
   }
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar + 1)));
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;\n" ::"r"(smem_u32(tslot)));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;\n" ::"r"(smem_u32(tslot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -424,98 +447,116 @@ __global__ void __launch_bounds__(128, 1)
 
   const int ntx = v.X / TX, ntz = v.Z / TC_TZ;
   const int ntiles = v.Y * ntz * ntx;
-  uint32_t phase = 0;
-  bool failed = false;
-  for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+  const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const int nstages = 3 * my_tiles;
+
+  // stage s = (tile blockIdx.x + (s / 3) gridDim.x, dy = s % 3) into buffer s % 2
+  auto stage = [&](int st) {
+    const int tile = blockIdx.x + (st / 3) * gridDim.x, dy = st % 3;
     const int xt = tile % ntx, rest = tile / ntx, zt = rest % ntz, y = rest / ntz;
     const int x0 = xt * TX, z0 = zt * TC_TZ;
-    // stage the three x-shifted halo copies
-    for (int c = threadIdx.x; c < 3 * TC_ROWS * KC; c += blockDim.x) {
-      const int kc = c % KC, row = (c / KC) % TC_ROWS, dx = c / (KC * TC_ROWS);
-      const int x = row % TX, zz = (row / TX) % TC_ZR, dy = row / (TX * TC_ZR);
-      const int gy = y + dy - 1;
-      const bool ok = gy >= 0 && gy < v.Y;
-      const int gz = (z0 + zz - 1 + v.Z) % v.Z, gx = (x0 + x + dx - 1 + v.X) % v.X;
+    const int gy = y + dy - 1;
+    const bool ok = gy >= 0 && gy < v.Y;
+    uint4* buf = sA + (size_t)(st & 1) * A_BUF;
+    for (int c = threadIdx.x; c < UNITS * KC; c += blockDim.x) {
+      const int kc = c & (KC - 1), unit = c >> LKC;
+      const int x = unit & (TX - 1), r = unit >> 5;    // r = dx * TC_ZR + zz
+      const int dx = r / TC_ZR, zz = r - dx * TC_ZR;
+      int gz = z0 + zz - 1, gx = x0 + x + dx - 1;
+      gz = gz < 0 ? gz + v.Z : (gz >= v.Z ? gz - v.Z : gz);
+      gx = gx < 0 ? gx + v.X : (gx >= v.X ? gx - v.X : gx);
       const size_t vox = ok ? ((size_t)gy * v.Z + gz) * v.X + gx : 0;
-      cp_async16(sA + (size_t)dx * A_COPY + (size_t)kc * TC_ROWS + row, in + vox * CIN + kc * 8, ok);
+      cp_async16(buf + (size_t)dx * A_SHIFT + (size_t)kc * TC_PLANE + zz * TX + x, in + vox * CIN + kc * 8, ok);
     }
-    cp_async_wait_all();
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
+
+  bool failed = false;
+  if (nstages > 0) stage(0);
+  for (int s = 0; s < nstages && !failed; ++s) {
+    const int dy = s % 3;
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");       // stage s is in shared memory
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // generic-proxy writes -> tensor core reads
     __syncthreads();
     if (threadIdx.x == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      for (int tap = 0; tap < 27; ++tap) {
-        const int dy = tap / 9, dz = (tap / 3) % 3, dx = tap % 3;
-        const uint32_t a0 = smem_u32(sA + (size_t)dx * A_COPY + (size_t)(dy * TC_ZR + dz) * TX);
+      const uint4* buf = sA + (size_t)(s & 1) * A_BUF;
+      for (int t = 0; t < 9; ++t) {
+        const int dz = t / 3, dx = t % 3, tap = dy * 9 + t;
         const uint32_t b0 = smem_u32(sB + (size_t)tap * KC * COUT);
 #pragma unroll
         for (int ks = 0; ks < CIN / 16; ++ks) {
-          const uint64_t ad = tc_smem_desc(a0 + ks * 2 * A_LBO, A_LBO, 128);
           const uint64_t bd = tc_smem_desc(b0 + ks * 2 * B_LBO, B_LBO, 128);
-          const uint32_t acc = (tap > 0 || ks > 0) ? 1u : 0u;
-          asm volatile(
-              "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-              "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+          const uint32_t acc = (dy > 0 || t > 0 || ks > 0) ? 1u : 0u;
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {  // z rows 4h .. 4h+3 of the tile
+            const uint32_t a0 = smem_u32(buf + (size_t)dx * A_SHIFT + (size_t)(2 * ks) * TC_PLANE + (dz + 4 * h) * TX);
+            const uint64_t ad = tc_smem_desc(a0, A_LBO, 128);
+            asm volatile(
+                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem + (uint32_t)(h * 32)),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+          }
         }
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-          smem_u32(bar)));
+          smem_u32(bar + (s & 1))));
     }
-    // every thread waits for the accumulator (bounded)
-    uint32_t done = 0;
-    for (unsigned it = 0; it < kTcSpinLimit && !done; ++it) {
-      asm volatile(
-          "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-          : "=r"(done)
-          : "r"(smem_u32(bar)), "r"(phase));
+    if (s + 1 < nstages) {
+      // buffer (s+1) % 2 was read by stage s-1's MMAs: the (s-1)/2-th completion of its mbarrier
+      if (s >= 1 && !tc_wait(bar + ((s + 1) & 1), (uint32_t)(((s - 1) >> 1) & 1))) failed = true;
+      if (!failed) stage(s + 1);
     }
-    if (!done) {
-      if (threadIdx.x == 0) atomicExch(err, 1);
-      failed = true;
-    }
-    phase ^= 1u;
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    if (!failed) {
-      // row m = 32 warp + lane of the accumulator: voxel (z row = warp, x = lane)
-      uint32_t r[32];
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
-            "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
-            "=r"(r[30]), "=r"(r[31])
-          : "r"(taddr));
-      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-      const size_t vox = ((size_t)y * v.Z + z0 + warp) * v.X + x0 + lane;
+    if (dy == 2 && !failed) {  // the tile's accumulators are complete once stage s's MMAs are
+      if (!tc_wait(bar + (s & 1), (uint32_t)((s >> 1) & 1))) failed = true;
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      if (!failed) {
+        const int tile = blockIdx.x + (s / 3) * gridDim.x;
+        const int xt = tile % ntx, rest = tile / ntx, zt = rest % ntz, y = rest / ntz;
+        const int g = warp & 3, h = warp >> 2;
+        uint32_t r[32];
+        const uint32_t taddr = tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(h * 32);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+              "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+              "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+              "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        const size_t vox = ((size_t)y * v.Z + zt * TC_TZ + 4 * h + g) * v.X + xt * TX + lane;
 #pragma unroll
-      for (int n = 0; n < COUT; n += 2) {
-        float r0 = __uint_as_float(r[n]), r1 = __uint_as_float(r[n + 1]);
-        if (epi & EPI_BIAS) { r0 += bias[n]; r1 += bias[n + 1]; }
-        if (epi & EPI_RELU) { r0 = fmaxf(r0, 0.f); r1 = fmaxf(r1, 0.f); }
-        if (epi & EPI_GATE) {
-          const __nv_bfloat162 gv = *reinterpret_cast<const __nv_bfloat162*>(gate + vox * COUT + n);
-          if (!(__low2float(gv) > 0.f)) r0 = 0.f;
-          if (!(__high2float(gv) > 0.f)) r1 = 0.f;
+        for (int n = 0; n < COUT; n += 2) {
+          float r0 = __uint_as_float(r[n]), r1 = __uint_as_float(r[n + 1]);
+          if (epi & EPI_BIAS) { r0 += bias[n]; r1 += bias[n + 1]; }
+          if (epi & EPI_RELU) { r0 = fmaxf(r0, 0.f); r1 = fmaxf(r1, 0.f); }
+          if (epi & EPI_GATE) {
+            const __nv_bfloat162 gv = *reinterpret_cast<const __nv_bfloat162*>(gate + vox * COUT + n);
+            if (!(__low2float(gv) > 0.f)) r0 = 0.f;
+            if (!(__high2float(gv) > 0.f)) r1 = 0.f;
+          }
+          if (epi & EPI_RES) {
+            const __nv_bfloat162 rv = *reinterpret_cast<const __nv_bfloat162*>(res + vox * COUT + n);
+            r0 += __low2float(rv);
+            r1 += __high2float(rv);
+          }
+          store2<OutT>(out + vox * COUT + n, r0, r1);
         }
-        if (epi & EPI_RES) {
-          const __nv_bfloat162 rv = *reinterpret_cast<const __nv_bfloat162*>(res + vox * COUT + n);
-          r0 += __low2float(rv);
-          r1 += __high2float(rv);
-        }
-        store2<OutT>(out + vox * COUT + n, r0, r1);
       }
     }
+    // one decision for the whole CTA (a wait that ran out anywhere ends every thread's loop), and the
+    // barrier after which the next tile's first MMAs may overwrite the accumulators every warp has read
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();  // accumulator read and halo copies consumed before the next tile
+    failed = __syncthreads_or(failed ? 1 : 0) != 0;
   }
-  cp_async_wait_all();
+  if (failed && threadIdx.x == 0) atomicExch(err, 1);
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;\n" ::"r"(tmem));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;\n" ::"r"(tmem));
 }
 
 // ---- launchers ---------------------------------------------------------------
@@ -531,7 +572,7 @@ __device__ int g_tc_err;  // set when a tcgen05 convolution's mbarrier wait ran 
 
 template <int CIN, int COUT>
 constexpr size_t tc_smem() {
-  return (size_t)3 * (CIN / 8) * TC_ROWS * 16 + (size_t)27 * (CIN / 8) * COUT * 16 + 16;
+  return (size_t)2 * 3 * (CIN / 8) * TC_PLANE * 16 + (size_t)27 * (CIN / 8) * COUT * 16 + 32;
 }
 
 template <int CIN, int COUT, typename OutT>
@@ -546,7 +587,7 @@ cudaError_t conv_fwd_tc(const void* in, const void* w, const float* bias, void* 
   if (e != cudaSuccess) return e;
   const int ntiles = v.Y * (v.Z / TC_TZ) * (v.X / TX);
   const int grid = ntiles < num_sms() ? ntiles : num_sms();
-  k<<<grid, 128, sm, st>>>((const __nv_bfloat16*)in, (const __nv_bfloat16*)w, bias, (OutT*)out,
+  k<<<grid, TC_THREADS, sm, st>>>((const __nv_bfloat16*)in, (const __nv_bfloat16*)w, bias, (OutT*)out,
                            (const __nv_bfloat16*)res, (const __nv_bfloat16*)gate, epi, v, err);
   return cudaGetLastError();
 }
@@ -638,7 +679,7 @@ int lh_sr_conv_fwd_tc(int32_t cin, int32_t cout, const void* in, const void* w, 
   int rc = sr_check_vol(X, Y, Z);
   if (rc) return rc;
   if (Z % lh::sr::TC_TZ) {
-    lh::set_init_error("lh_sr_conv_fwd_tc: Z must be a multiple of 4");
+    lh::set_init_error("lh_sr_conv_fwd_tc: Z must be a multiple of 8");
     return LH_EINVAL;
   }
   if (!in || !w || !out || !aligned16(in) || !aligned16(w) || ((flags & 2) && !res) || ((flags & 4) && !gate) ||

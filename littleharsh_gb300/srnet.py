@@ -138,7 +138,7 @@ class SRNet:
         co = cout if cout is not None else vw["co"]
         w = weights if weights is not None else vw["w"]
         Y, Z, X = self._shape
-        fn = L.lh_sr_conv_fwd_tc if (self.tcgen05 and Z % 4 == 0) else L.lh_sr_conv_fwd
+        fn = L.lh_sr_conv_fwd_tc if (self.tcgen05 and Z % 8 == 0) else L.lh_sr_conv_fwd
         _check(fn(ci, co, _ptr(x), _ptr(w), _ptr(vw["b"]) if flags & BIAS else None, _ptr(out),
                   int(out_f32), _ptr(res), _ptr(gate), flags, X, Y, Z, _stream()), "lh_sr_conv_fwd")
 

@@ -264,3 +264,25 @@ def test_conv_fwd_tcgen05(lib, cin, cout, f32, flags):
         np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5)
     else:
         np.testing.assert_allclose(got, ref, rtol=2 ** -8, atol=1e-3)
+
+
+@pytest.mark.gpu
+def test_conv_fwd_tcgen05_many_tiles_per_cta(lib):
+    """More tiles than SMs: each persistent CTA pipelines several tiles through its two stage buffers."""
+    import ctypes
+    import torch
+    from littleharsh_gb300 import srnet
+    rng = np.random.default_rng(77)
+    Y, Z, X = 80, 16, 64  # 320 tiles of 8 z-rows x 32 x-voxels
+    x = so.bf16_round(rng.standard_normal((Y, Z, X, 32)))
+    w = so.bf16_round(rng.standard_normal((27, 32, 32)) / np.sqrt(27 * 32))
+    b = rng.standard_normal(32).astype(np.float32)
+    ref = so.conv_fwd(x, w, b, flags=so.BIAS | so.RELU)
+    out = torch.empty((Y, Z, X, 32), dtype=torch.bfloat16, device="cuda")
+    xt, wt, bt = _t(x, torch.bfloat16), _t(w, torch.bfloat16), _t(b, torch.float32)
+    assert lib.lh_sr_conv_fwd_tc(32, 32, srnet._ptr(xt), srnet._ptr(wt), srnet._ptr(bt), srnet._ptr(out), 0, None,
+                                 None, so.BIAS | so.RELU, X, Y, Z, None) == 0
+    torch.cuda.synchronize()
+    timed_out = ctypes.c_int32(-1)
+    assert lib.lh_sr_tc_status(ctypes.byref(timed_out)) == 0 and timed_out.value == 0
+    np.testing.assert_allclose(out.float().cpu().numpy(), ref, rtol=2 ** -8, atol=1e-3)
