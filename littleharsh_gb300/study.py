@@ -374,8 +374,6 @@ def main(argv=None):
                           "val": res["training"]["history"][-1]}))
 
 
-if __name__ == "__main__":
-    main()
 
 
 STAT_KEYS = ("U", "urms", "vrms", "wrms", "uv")
@@ -497,3 +495,7 @@ def precision_ensemble(cfg: dict, realisations: int = 3, re_tau: float = 180.0, 
     for s in sols:
         s.close()
     return res
+
+
+if __name__ == "__main__":
+    main()
