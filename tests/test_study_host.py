@@ -47,3 +47,14 @@ def test_stationarity_measures():
     assert study.stationary_from(recs, devs, 0.001, 2) is None
     # a run that only settles in its last window has not stayed settled
     assert study.stationary_from(recs, [1.0] * 19 + [0.0], 0.5, 2) is None
+
+
+def test_command_line_runs_after_every_definition():
+    """`python -m littleharsh_gb300.study` calls main() from the module's last statement, so every
+    function main() dispatches to exists by then."""
+    import ast
+    import inspect
+    tree = ast.parse(inspect.getsource(study))
+    last = tree.body[-1]
+    assert isinstance(last, ast.If) and "__main__" in ast.unparse(last.test)
+    assert not any(isinstance(n, (ast.FunctionDef, ast.ClassDef)) for n in tree.body[tree.body.index(last):])
