@@ -360,26 +360,30 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
 
 // ---- tcgen05 forward convolution ------------------------------------------------
 //
-// The same convolution on the 5th-generation tensor cores.  A tile is 8 z-rows
-// x 32 x-voxels of one y level (M = 256 as two M = 128 halves, two fp32
-// accumulators of Cout columns in TMEM).  Its work runs as three stages, one
-// per y offset dy of the taps: a stage stages the dy level's halo (10 z-rows x
-// 32 voxels for each of the three x shifts, so that the A operand of a tap is
-// 128 consecutive rows, i.e. a start address) into one of two shared-memory
-// buffers, then one elected thread issues the stage's 9 taps x Cin/16 x 2
-// tcgen05.mma (K = 16 channels, bf16 operands from shared memory) and commits
-// them to the buffer's mbarrier.  While the tensor cores work on stage s, all
-// threads stage s + 1 into the other buffer (after that buffer's previous MMAs
-// completed), so staging and MMAs overlap across stages and tiles.  After a
-// tile's last stage eight warps read the accumulators back with tcgen05.ld
-// (warp w: TMEM lanes 32 (w mod 4), half w / 4) for the epilogue.
-// Operands use the no-swizzle K-major layout (core matrices of 8 rows x 16
-// bytes, rows 16 bytes apart): A rows [x shift][k chunk][z row][x] with the
-// k-chunk planes padded by 2 rows against bank conflicts; weights rows
-// [tap][k chunk][cout].  Every mbarrier wait is bounded.
+// The same convolution on the 5th-generation tensor cores.  A tile is 32
+// x-voxels x 8 z-rows of one y level (M = 256 as two M = 128 halves of 16
+// x-voxels, fp32 accumulators of Cout columns in TMEM).  Its work runs as three
+// stages, one per y offset dy of the taps.  A stage's input is the dy level's
+// halo, 34 x-voxels x 10 z-rows, held in shared memory as 16-byte rows
+// [k chunk][x][z] (no-swizzle K-major core matrices of 8 rows x 16 bytes).
+// With z fastest, a core matrix is 8 consecutive z of one x, and consecutive
+// core matrices along M are consecutive x, 10 rows apart; the A operand of tap
+// (dz, dx) is then the same layout started dz + 10 dx rows further on, so the
+// nine taps of a stage read one halo copy through their descriptors' start
+// addresses and nothing is copied twice.  Halos are fetched with cp.async into
+// a ring of four buffers, up to three stages ahead.  One thread issues a
+// stage's 9 taps x Cin/16 x 2 tcgen05.mma (K = 16 channels, bf16 operands from
+// shared memory) and commits them to the buffer's mbarrier, whose completion
+// frees the buffer for the halo four stages on.  The accumulators are
+// double-buffered in TMEM (128 columns), so a tile's epilogue (eight warps,
+// tcgen05.ld of TMEM lanes 32 (w mod 4), half w / 4) runs while the tensor
+// cores work on the next tile.  Weights rows: [tap][k chunk][cout].  Every
+// mbarrier wait is bounded.
 constexpr int TC_TZ = 8;                     // z rows per tile
-constexpr int TC_ZR = TC_TZ + 2;             // staged z rows per dy
-constexpr int TC_PLANE = TC_ZR * TX + 2;     // 16-byte rows per k-chunk plane (2 rows of padding)
+constexpr int TC_ZR = TC_TZ + 2;             // halo z rows
+constexpr int TC_XR = TX + 2;                // halo x voxels
+constexpr int TC_HALO = TC_ZR * TC_XR;       // 16-byte rows per k-chunk plane of a halo
+constexpr int TC_NBUF = 4;                   // halo ring
 constexpr int TC_THREADS = 256;
 constexpr unsigned kTcSpinLimit = 1u << 20;  // bound of every mbarrier wait
 
@@ -413,17 +417,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                   const float* __restrict__ bias, OutT* __restrict__ out, const __nv_bfloat16* __restrict__ res,
                   const __nv_bfloat16* __restrict__ gate, int epi, Vol v, int* __restrict__ err) {
   constexpr int KC = CIN / 8;                       // 16-byte chunks (core-matrix columns) per voxel row
-  constexpr int LKC = KC == 4 ? 2 : 1;              // log2 KC (CIN = 32 or 16)
-  constexpr uint32_t A_LBO = TC_PLANE * 16;         // next k chunk of an x-shift copy
+  constexpr uint32_t A_LBO = TC_HALO * 16;          // next k chunk of a halo
+  constexpr uint32_t A_SBO = TC_ZR * 16;            // next 8 rows along M = next x
   constexpr uint32_t B_LBO = COUT * 16;             // next k chunk of a tap's weights
-  constexpr int A_SHIFT = KC * TC_PLANE;            // 16-byte rows per x-shift copy
-  constexpr int A_BUF = 3 * A_SHIFT;                // rows per stage buffer
-  constexpr int UNITS = 3 * TC_ZR * TX;             // voxel rows staged per stage
+  constexpr int BUF = KC * TC_HALO;                 // 16-byte rows per halo buffer
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint4* sA = reinterpret_cast<uint4*>(smem_raw);   // [2 buffers][3 dx][KC][TC_PLANE]
-  uint4* sB = sA + 2 * A_BUF;                       // [27][KC][COUT]
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sB + (size_t)27 * KC * COUT);  // one per buffer
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
+  uint4* sA = reinterpret_cast<uint4*>(smem_raw);   // [TC_NBUF][KC][TC_XR][TC_ZR]
+  uint4* sB = sA + (size_t)TC_NBUF * BUF;           // [27][KC][COUT]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sB + (size_t)27 * KC * COUT);  // one per halo buffer
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + TC_NBUF);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
   for (int c = threadIdx.x; c < 27 * COUT * KC; c += blockDim.x) {  // weights -> [27][KC][COUT] rows
@@ -431,12 +433,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     cp_async16(sB + ((size_t)tap * KC + kc) * COUT + n, w + ((size_t)tap * COUT + n) * CIN + kc * 8, true);
   }
   if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar)));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar + 1)));
+    for (int b = 0; b < TC_NBUF; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar + b)));
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;\n" ::"r"(smem_u32(tslot)));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;\n" ::"r"(smem_u32(tslot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -450,37 +451,82 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
   const int nstages = 3 * my_tiles;
 
-  // stage s = (tile blockIdx.x + (s / 3) gridDim.x, dy = s % 3) into buffer s % 2
-  auto stage = [&](int st) {
-    const int tile = blockIdx.x + (st / 3) * gridDim.x, dy = st % 3;
-    const int xt = tile % ntx, rest = tile / ntx, zt = rest % ntz, y = rest / ntz;
-    const int x0 = xt * TX, z0 = zt * TC_TZ;
-    const int gy = y + dy - 1;
-    const bool ok = gy >= 0 && gy < v.Y;
-    uint4* buf = sA + (size_t)(st & 1) * A_BUF;
-    for (int c = threadIdx.x; c < UNITS * KC; c += blockDim.x) {
-      const int kc = c & (KC - 1), unit = c >> LKC;
-      const int x = unit & (TX - 1), r = unit >> 5;    // r = dx * TC_ZR + zz
-      const int dx = r / TC_ZR, zz = r - dx * TC_ZR;
-      int gz = z0 + zz - 1, gx = x0 + x + dx - 1;
-      gz = gz < 0 ? gz + v.Z : (gz >= v.Z ? gz - v.Z : gz);
-      gx = gx < 0 ? gx + v.X : (gx >= v.X ? gx - v.X : gx);
-      const size_t vox = ok ? ((size_t)gy * v.Z + gz) * v.X + gx : 0;
-      cp_async16(buf + (size_t)dx * A_SHIFT + (size_t)kc * TC_PLANE + zz * TX + x, in + vox * CIN + kc * 8, ok);
+  // the halo of stage st = (tile blockIdx.x + (st / 3) gridDim.x, dy = st % 3) into buffer st % TC_NBUF:
+  // rows [k chunk][x + 1][z + 1], x = -1 .. 32, z = -1 .. 8, periodic in x and z, zero outside y;
+  // every call commits one cp.async group (an empty one past the last stage)
+  auto fetch = [&](int st) {
+    if (st < nstages) {
+      const int tile = blockIdx.x + (st / 3) * gridDim.x, dy = st % 3;
+      const int xt = tile % ntx, rest = tile / ntx, zt = rest % ntz, y = rest / ntz;
+      const int x0 = xt * TX, z0 = zt * TC_TZ;
+      const int gy = y + dy - 1;
+      const bool ok = gy >= 0 && gy < v.Y;
+      uint4* buf = sA + (size_t)(st % TC_NBUF) * BUF;
+      for (int c = threadIdx.x; c < TC_HALO * KC; c += blockDim.x) {
+        const int kc = c % KC, u = c / KC;
+        const int xh = u % TC_XR, zz = u / TC_XR;
+        int gz = z0 + zz - 1, gx = x0 + xh - 1;
+        gz = gz < 0 ? gz + v.Z : (gz >= v.Z ? gz - v.Z : gz);
+        gx = gx < 0 ? gx + v.X : (gx >= v.X ? gx - v.X : gx);
+        const size_t vox = ok ? ((size_t)gy * v.Z + gz) * v.X + gx : 0;
+        cp_async16(buf + ((size_t)kc * TC_XR + xh) * TC_ZR + zz, in + vox * CIN + kc * 8, ok);
+      }
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
   };
 
+  // the epilogue of this CTA's tile ti from accumulator set ti % 2: warp w reads TMEM lanes
+  // 32 (w mod 4) .. +31 of half w / 4; lane m of half h is the voxel x = 16 h + m / 8, z = m mod 8
+  auto epilogue = [&](int ti) {
+    const int tile = blockIdx.x + ti * gridDim.x;
+    const int xt = tile % ntx, rest = tile / ntx, zt = rest % ntz, y = rest / ntz;
+    const int g = warp & 3, h = warp >> 2;
+    uint32_t r[32];
+    const uint32_t taddr = tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)((ti & 1) * 64 + h * 32);
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+          "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+          "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+    const int m = g * 32 + lane;
+    const size_t vox = ((size_t)y * v.Z + zt * TC_TZ + (m & 7)) * v.X + xt * TX + 16 * h + (m >> 3);
+#pragma unroll
+    for (int n = 0; n < COUT; n += 2) {
+      float r0 = __uint_as_float(r[n]), r1 = __uint_as_float(r[n + 1]);
+      if (epi & EPI_BIAS) { r0 += bias[n]; r1 += bias[n + 1]; }
+      if (epi & EPI_RELU) { r0 = fmaxf(r0, 0.f); r1 = fmaxf(r1, 0.f); }
+      if (epi & EPI_GATE) {
+        const __nv_bfloat162 gv = *reinterpret_cast<const __nv_bfloat162*>(gate + vox * COUT + n);
+        if (!(__low2float(gv) > 0.f)) r0 = 0.f;
+        if (!(__high2float(gv) > 0.f)) r1 = 0.f;
+      }
+      if (epi & EPI_RES) {
+        const __nv_bfloat162 rv = *reinterpret_cast<const __nv_bfloat162*>(res + vox * COUT + n);
+        r0 += __low2float(rv);
+        r1 += __high2float(rv);
+      }
+      store2<OutT>(out + vox * COUT + n, r0, r1);
+    }
+  };
+
   bool failed = false;
-  if (nstages > 0) stage(0);
-  for (int s = 0; s < nstages && !failed; ++s) {
-    const int dy = s % 3;
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");       // stage s is in shared memory
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // generic-proxy writes -> tensor core reads
+  int issued = 0;  // stages whose MMAs were issued
+  for (int q = 0; q < TC_NBUF - 1; ++q) fetch(q);
+  for (int s = 0; s < nstages; ++s) {
+    const int dy = s % 3, ti = s / 3;
+    // groups committed so far: stages 0 .. s + TC_NBUF - 2; all but the newest TC_NBUF - 2 have landed
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(TC_NBUF - 2) : "memory");
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // cp.async writes -> tensor core reads
     __syncthreads();
     if (threadIdx.x == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      const uint4* buf = sA + (size_t)(s & 1) * A_BUF;
+      const uint32_t a_base = smem_u32(sA + (size_t)(s % TC_NBUF) * BUF);
+      const uint32_t d_base = tmem + (uint32_t)((ti & 1) * 64);
       for (int t = 0; t < 9; ++t) {
         const int dz = t / 3, dx = t % 3, tap = dy * 9 + t;
         const uint32_t b0 = smem_u32(sB + (size_t)tap * KC * COUT);
@@ -489,74 +535,53 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           const uint64_t bd = tc_smem_desc(b0 + ks * 2 * B_LBO, B_LBO, 128);
           const uint32_t acc = (dy > 0 || t > 0 || ks > 0) ? 1u : 0u;
 #pragma unroll
-          for (int h = 0; h < 2; ++h) {  // z rows 4h .. 4h+3 of the tile
-            const uint32_t a0 = smem_u32(buf + (size_t)dx * A_SHIFT + (size_t)(2 * ks) * TC_PLANE + (dz + 4 * h) * TX);
-            const uint64_t ad = tc_smem_desc(a0, A_LBO, 128);
+          for (int h = 0; h < 2; ++h) {  // x-voxels 16h .. 16h+15 of the tile
+            const uint32_t a0 = a_base + (uint32_t)((2 * ks * TC_HALO + (16 * h + dx) * TC_ZR + dz) * 16);
+            const uint64_t ad = tc_smem_desc(a0, A_LBO, A_SBO);
             asm volatile(
                 "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem + (uint32_t)(h * 32)),
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_base + (uint32_t)(h * 32)),
                 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
           }
         }
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-          smem_u32(bar + (s & 1))));
+          smem_u32(bar + s % TC_NBUF)));
     }
-    if (s + 1 < nstages) {
-      // buffer (s+1) % 2 was read by stage s-1's MMAs: the (s-1)/2-th completion of its mbarrier
-      if (s >= 1 && !tc_wait(bar + ((s + 1) & 1), (uint32_t)(((s - 1) >> 1) & 1))) failed = true;
-      if (!failed) stage(s + 1);
+    issued = s + 1;
+    if (s >= 1) {
+      // stage s-1's MMAs (the (s-1)/TC_NBUF-th completion of its buffer's mbarrier) have read their halo and,
+      // when s begins a tile, finished the previous tile's accumulators; one decision for the whole CTA
+      const int q = s - 1;
+      const bool ok = tc_wait(bar + q % TC_NBUF, (uint32_t)((q / TC_NBUF) & 1));
+      failed = __syncthreads_or(ok ? 0 : 1) != 0;
+      if (failed) break;
     }
-    if (dy == 2 && !failed) {  // the tile's accumulators are complete once stage s's MMAs are
-      if (!tc_wait(bar + (s & 1), (uint32_t)((s >> 1) & 1))) failed = true;
+    fetch(s + TC_NBUF - 1);  // into buffer (s - 1) % TC_NBUF, free since the wait above
+    if (dy == 0 && ti >= 1) {
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      if (!failed) {
-        const int tile = blockIdx.x + (s / 3) * gridDim.x;
-        const int xt = tile % ntx, rest = tile / ntx, zt = rest % ntz, y = rest / ntz;
-        const int g = warp & 3, h = warp >> 2;
-        uint32_t r[32];
-        const uint32_t taddr = tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(h * 32);
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-              "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
-              "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
-              "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-            : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        const size_t vox = ((size_t)y * v.Z + zt * TC_TZ + 4 * h + g) * v.X + xt * TX + lane;
-#pragma unroll
-        for (int n = 0; n < COUT; n += 2) {
-          float r0 = __uint_as_float(r[n]), r1 = __uint_as_float(r[n + 1]);
-          if (epi & EPI_BIAS) { r0 += bias[n]; r1 += bias[n + 1]; }
-          if (epi & EPI_RELU) { r0 = fmaxf(r0, 0.f); r1 = fmaxf(r1, 0.f); }
-          if (epi & EPI_GATE) {
-            const __nv_bfloat162 gv = *reinterpret_cast<const __nv_bfloat162*>(gate + vox * COUT + n);
-            if (!(__low2float(gv) > 0.f)) r0 = 0.f;
-            if (!(__high2float(gv) > 0.f)) r1 = 0.f;
-          }
-          if (epi & EPI_RES) {
-            const __nv_bfloat162 rv = *reinterpret_cast<const __nv_bfloat162*>(res + vox * COUT + n);
-            r0 += __low2float(rv);
-            r1 += __high2float(rv);
-          }
-          store2<OutT>(out + vox * COUT + n, r0, r1);
-        }
-      }
+      epilogue(ti - 1);  // overlaps stage s's MMAs, which accumulate into the other set
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     }
-    // one decision for the whole CTA (a wait that ran out anywhere ends every thread's loop), and the
-    // barrier after which the next tile's first MMAs may overwrite the accumulators every warp has read
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    failed = __syncthreads_or(failed ? 1 : 0) != 0;
+  }
+  if (!failed && nstages > 0) {  // the last tile
+    const int q = nstages - 1;
+    const bool ok = tc_wait(bar + q % TC_NBUF, (uint32_t)((q / TC_NBUF) & 1));
+    failed = __syncthreads_or(ok ? 0 : 1) != 0;
+    if (!failed) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      epilogue(my_tiles - 1);
+    }
   }
   if (failed && threadIdx.x == 0) atomicExch(err, 1);
+  // MMAs still in flight after a wait ran out: wait (bounded) for the last issued stage, whose commit
+  // follows every earlier MMA, before the accumulators are freed
+  if (failed && issued > 0) tc_wait(bar + (issued - 1) % TC_NBUF, (uint32_t)(((issued - 1) / TC_NBUF) & 1));
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;\n" ::"r"(tmem));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;\n" ::"r"(tmem));
 }
 
 // ---- launchers ---------------------------------------------------------------
@@ -572,7 +597,7 @@ __device__ int g_tc_err;  // set when a tcgen05 convolution's mbarrier wait ran 
 
 template <int CIN, int COUT>
 constexpr size_t tc_smem() {
-  return (size_t)2 * 3 * (CIN / 8) * TC_PLANE * 16 + (size_t)27 * (CIN / 8) * COUT * 16 + 32;
+  return (size_t)TC_NBUF * (CIN / 8) * TC_HALO * 16 + (size_t)27 * (CIN / 8) * COUT * 16 + TC_NBUF * 8 + 16;
 }
 
 template <int CIN, int COUT, typename OutT>
