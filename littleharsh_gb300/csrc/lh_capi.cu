@@ -165,7 +165,12 @@ int build_plan(lh_handle* h, PlanStore& ps, int n, int keep_half) {
   if (s > kMaxStages) return fail(h, LH_EFFT, "transform length %d needs too many stages", n);
   P.ns = s;
   int L = 1;
-  for (int i = 0; i < s; ++i) { L *= P.rad[i]; P.len[i] = L; }
+  for (int i = 0; i < s; ++i) {
+    L *= P.rad[i];
+    P.len[i] = L;
+    P.mdiv[i] = fdiv_mult((unsigned)(L / P.rad[i]));
+    P.qdiv[i] = fdiv_mult((unsigned)(n / P.rad[i]));
+  }
   // the output slots a truncation keeps are [0, keep_half) and [n - keep_half, n)
   P.prune_mid = (s > 0 && P.rad[s - 1] == 3 && keep_half > 0 && keep_half * 3 == n) ? 1 : 0;
   std::vector<int> perm(n);

@@ -33,6 +33,8 @@ struct FftPlan {
   int rad[kMaxStages];    // radix of stage s (radix 4 first: stage 0 needs no twiddles; radix 3 last)
   int len[kMaxStages];    // transform length produced by stage s (len[ns-1] = n)
   int prune_mid;          // last stage is radix 3 over n/3 and the middle third of the output is not needed
+  unsigned mdiv[kMaxStages];  // ceil(2^32 / (len[s] / rad[s])) (0 for 1): divides by a stage's butterfly span
+  unsigned qdiv[kMaxStages];  // ceil(2^32 / (n / rad[s])) (0 for 1): divides by a stage's butterfly count
   const int* perm;        // device: position of sample n at the start (digit reversal)
   const double2* tw64;    // device: exp(-2 pi i k/n), k = 0..n-1
   const float2* tw32;     // same, rounded to float
@@ -123,31 +125,80 @@ __device__ __forceinline__ void dit_butterfly(cpx_t<R>* base, int st, int r, int
   }
 }
 
+// floor(t / d) for t * d < 2^32 as one multiply-high by mult = ceil(2^32 / d) (d > 1); d = 1 passes
+// t through.  Exact: t (mult - 2^32 / d) / 2^32 < t / 2^32 < 1 / d, less than the gap between t / d and
+// the next integer.
+__host__ __device__ __forceinline__ unsigned fdiv_mult(unsigned d) {
+  return d > 1 ? 0xFFFFFFFFu / d + 1u : 0u;  // = ceil(2^32 / d) for d > 1
+}
+__device__ __forceinline__ int fdiv(int t, int d, unsigned mult) {
+  return d > 1 ? (int)__umulhi((unsigned)t, mult) : t;
+}
+
+// One DIT stage of radix RADIX over `nb` vectors (see fft_dit).
+template <typename R, int SIGN, bool BFAST, int RADIX>
+__device__ __forceinline__ void dit_stage(cpx_t<R>* buf, int nb, unsigned nbm, int es, int bs, int L, int n,
+                                          unsigned mm, unsigned nbfm, bool skip_mid,
+                                          const cpx_t<R>* __restrict__ tw) {
+  const int m = L / RADIX, ts = n / L;
+  const int nbf = n / RADIX;
+  const int total = nb * nbf;
+  const bool twiddle = m > 1;
+  const int q = BFAST ? nb : nbf;  // the divisor that splits t into (vector, butterfly)
+  const unsigned qm = BFAST ? nbm : nbfm;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    int b, f;
+    if (BFAST) { f = fdiv(t, q, qm); b = t - f * nb; }
+    else { b = fdiv(t, q, qm); f = t - b * nbf; }
+    const int blk = fdiv(f, m, mm), k = f - blk * m;
+    cpx_t<R>* base = buf + b * bs + (blk * L + k) * es;
+    dit_butterfly<R, SIGN>(base, m * es, RADIX, k * ts, twiddle, skip_mid, tw);
+  }
+}
+
 // In-place DIT over `nb` vectors: element e of vector b at buf[b*bs + e*es].
 // BFAST: consecutive threads take consecutive vectors (for interleaved
 // vectors, es = nb-ish, bs = 1); otherwise consecutive butterflies of one
 // vector (es = 1).  SIGN = -1 forward, +1 inverse; no normalisation.
 // prune: skip the middle output third of the last radix-3 stage.
+// FP32: the radix is resolved once per stage, so each stage's loop runs one
+// butterfly form with its index divisions as multiply-highs; the FP32
+// transforms are bound by instruction issue, and this halves the integer work
+// per butterfly.  FP64: one loop over all radices with plain divisions, which
+// measures faster on the FP64 pipe, where the integer work runs alongside.
 template <typename R, int SIGN, bool BFAST>
 __device__ void fft_dit(cpx_t<R>* buf, int nb, int es, int bs, const FftPlan& P, bool prune) {
   using T2 = cpx_t<R>;
   const T2* __restrict__ tw = twtab<R>(P);
   const int n = P.n;
-  for (int s = 0; s < P.ns; ++s) {
-    const int r = P.rad[s], L = P.len[s], m = L / r, ts = n / L;
-    const int nbf = n / r;
-    const int total = nb * nbf;
-    const bool twiddle = m > 1;
-    const bool skip_mid = prune && s == P.ns - 1;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      int b, f;
-      if (BFAST) { f = t / nb; b = t - f * nb; }
-      else { b = t / nbf; f = t - b * nbf; }
-      const int blk = f / m, k = f - blk * m;
-      T2* base = buf + b * bs + (blk * L + k) * es;
-      dit_butterfly<R, SIGN>(base, m * es, r, k * ts, twiddle, skip_mid, tw);
+  if constexpr (sizeof(R) == 4) {
+    const unsigned nbm = BFAST ? fdiv_mult((unsigned)nb) : 0u;
+    for (int s = 0; s < P.ns; ++s) {
+      const int r = P.rad[s], L = P.len[s];
+      const unsigned mm = P.mdiv[s], nbfm = P.qdiv[s];
+      const bool skip_mid = prune && s == P.ns - 1;
+      if (r == 4) dit_stage<R, SIGN, BFAST, 4>(buf, nb, nbm, es, bs, L, n, mm, nbfm, false, tw);
+      else if (r == 2) dit_stage<R, SIGN, BFAST, 2>(buf, nb, nbm, es, bs, L, n, mm, nbfm, false, tw);
+      else dit_stage<R, SIGN, BFAST, 3>(buf, nb, nbm, es, bs, L, n, mm, nbfm, skip_mid, tw);
+      __syncthreads();
     }
-    __syncthreads();
+  } else {
+    for (int s = 0; s < P.ns; ++s) {
+      const int r = P.rad[s], L = P.len[s], m = L / r, ts = n / L;
+      const int nbf = n / r;
+      const int total = nb * nbf;
+      const bool twiddle = m > 1;
+      const bool skip_mid = prune && s == P.ns - 1;
+      for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        int b, f;
+        if (BFAST) { f = t / nb; b = t - f * nb; }
+        else { b = t / nbf; f = t - b * nbf; }
+        const int blk = f / m, k = f - blk * m;
+        T2* base = buf + b * bs + (blk * L + k) * es;
+        dit_butterfly<R, SIGN>(base, m * es, r, k * ts, twiddle, skip_mid, tw);
+      }
+      __syncthreads();
+    }
   }
 }
 
