@@ -125,6 +125,79 @@ __device__ __forceinline__ void dit_butterfly(cpx_t<R>* base, int st, int r, int
   }
 }
 
+// One DIT butterfly of radix RADIX on values held in registers (the same
+// arithmetic as dit_butterfly); with skip_mid the radix-3 output v[1] is left
+// as it was.
+template <typename R, int SIGN, int RADIX>
+__device__ __forceinline__ void bfly(cpx_t<R>* v, int e, bool twiddle, bool skip_mid,
+                                     const cpx_t<R>* __restrict__ tw) {
+  using T2 = cpx_t<R>;
+  if constexpr (RADIX == 4) {
+    const T2 a = v[0], b = v[1], c = v[2], d = v[3];
+    T2 t0, t1, t2, t3;
+    if (twiddle) {
+      const T2 w1 = tw[e], w2 = tw[2 * e], w3 = tw[3 * e];
+      t0 = cmad<SIGN>(a, c, w2);
+      t1 = ctwice_minus(a, t0);
+      const T2 B = cmul<SIGN>(b, w1);
+      t2 = cmad<SIGN>(B, d, w3);
+      t3 = ctwice_minus(B, t2);
+    } else {
+      t0 = cadd(a, c); t1 = csub(a, c); t2 = cadd(b, d); t3 = csub(b, d);
+    }
+    const T2 u = cimul<SIGN>(t3);
+    v[0] = cadd(t0, t2);
+    v[1] = cadd(t1, u);
+    v[2] = csub(t0, t2);
+    v[3] = csub(t1, u);
+  } else if constexpr (RADIX == 2) {
+    const T2 a = v[0], b = v[1];
+    if (twiddle) {
+      const T2 s = cmad<SIGN>(a, b, tw[e]);
+      v[0] = s;
+      v[1] = ctwice_minus(a, s);
+    } else {
+      v[0] = cadd(a, b);
+      v[1] = csub(a, b);
+    }
+  } else {
+    const R s3 = (SIGN < 0) ? (R)-0.86602540378443864676 : (R)0.86602540378443864676;
+    const T2 a = v[0], b = v[1], c = v[2];
+    T2 t1, d;
+    if (twiddle) {
+      const T2 B = cmul<SIGN>(b, tw[e]);
+      t1 = cmad<SIGN>(B, c, tw[2 * e]);
+      d = ctwice_minus(B, t1);
+    } else {
+      t1 = cadd(b, c);
+      d = csub(b, c);
+    }
+    const T2 t2 = T2{fma((R)-0.5, t1.x, a.x), fma((R)-0.5, t1.y, a.y)};
+    v[0] = cadd(a, t1);
+    if (skip_mid) {
+      v[2] = T2{fma(s3, d.y, t2.x), fma(-s3, d.x, t2.y)};
+    } else {
+      const T2 x1 = T2{fma(-s3, d.y, t2.x), fma(s3, d.x, t2.y)};
+      v[1] = x1;
+      v[2] = ctwice_minus(t2, x1);
+    }
+  }
+}
+
+// Shared-memory slot of element i of an x-transform buffer.  FP32 buffers
+// hold one padding element after every 16: the digit-reversed input scatter
+// and the first DIT stages step through the buffer in multiples of 4 and 16
+// elements, which without padding meet in the same banks.  FP64 buffers are
+// unpadded.
+template <typename R> __device__ __forceinline__ int sxi(int i) {
+  if constexpr (sizeof(R) == 4) return i + (i >> 4);
+  else return i;
+}
+// elements to allocate for an x-transform buffer of n elements
+template <typename R> __host__ __device__ constexpr size_t sx_elems(size_t n) {
+  return sizeof(R) == 4 ? n + n / 16 + 1 : n;
+}
+
 // floor(t / d) for t * d < 2^32 as one multiply-high by mult = ceil(2^32 / d) (d > 1); d = 1 passes
 // t through.  Exact: t (mult - 2^32 / d) / 2^32 < t / 2^32 < 1 / d, less than the gap between t / d and
 // the next integer.
@@ -156,6 +229,29 @@ __device__ __forceinline__ void dit_stage(cpx_t<R>* buf, int nb, unsigned nbm, i
   }
 }
 
+// One DIT stage of radix RADIX over `nb` vectors of an FP32 x-transform buffer
+// (es = 1, padded slots), index divisions as multiply-highs.
+template <typename R, int SIGN, int RADIX>
+__device__ __forceinline__ void dit_stage_padded(cpx_t<R>* buf, int nb, int bs, int L, int n, unsigned mm,
+                                                 unsigned nbfm, bool skip_mid, const cpx_t<R>* __restrict__ tw) {
+  const int m = L / RADIX, ts = n / L;
+  const int nbf = n / RADIX;
+  const int total = nb * nbf;
+  const bool twiddle = m > 1;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int b = fdiv(t, nbf, nbfm), f = t - b * nbf;
+    const int blk = fdiv(f, m, mm), k = f - blk * m;
+    const int i0 = b * bs + blk * L + k;
+    cpx_t<R> v[RADIX];
+#pragma unroll
+    for (int p = 0; p < RADIX; ++p) v[p] = buf[sxi<R>(i0 + p * m)];
+    bfly<R, SIGN, RADIX>(v, k * ts, twiddle, skip_mid, tw);
+#pragma unroll
+    for (int p = 0; p < RADIX; ++p)
+      if (!(RADIX == 3 && skip_mid && p == 1)) buf[sxi<R>(i0 + p * m)] = v[p];
+  }
+}
+
 // In-place DIT over `nb` vectors: element e of vector b at buf[b*bs + e*es].
 // BFAST: consecutive threads take consecutive vectors (for interleaved
 // vectors, es = nb-ish, bs = 1); otherwise consecutive butterflies of one
@@ -163,8 +259,9 @@ __device__ __forceinline__ void dit_stage(cpx_t<R>* buf, int nb, unsigned nbm, i
 // prune: skip the middle output third of the last radix-3 stage.
 // FP32: the radix is resolved once per stage, so each stage's loop runs one
 // butterfly form with its index divisions as multiply-highs; the FP32
-// transforms are bound by instruction issue, and this halves the integer work
-// per butterfly.  FP64: one loop over all radices with plain divisions, which
+// transforms are bound by instruction issue and shared memory, and this halves
+// the integer work per butterfly.  FP32 x transforms (not BFAST; es = 1) use
+// the padded slots of sxi.  FP64: one loop over all radices with plain divisions, which
 // measures faster on the FP64 pipe, where the integer work runs alongside.
 template <typename R, int SIGN, bool BFAST>
 __device__ void fft_dit(cpx_t<R>* buf, int nb, int es, int bs, const FftPlan& P, bool prune) {
@@ -177,9 +274,15 @@ __device__ void fft_dit(cpx_t<R>* buf, int nb, int es, int bs, const FftPlan& P,
       const int r = P.rad[s], L = P.len[s];
       const unsigned mm = P.mdiv[s], nbfm = P.qdiv[s];
       const bool skip_mid = prune && s == P.ns - 1;
-      if (r == 4) dit_stage<R, SIGN, BFAST, 4>(buf, nb, nbm, es, bs, L, n, mm, nbfm, false, tw);
-      else if (r == 2) dit_stage<R, SIGN, BFAST, 2>(buf, nb, nbm, es, bs, L, n, mm, nbfm, false, tw);
-      else dit_stage<R, SIGN, BFAST, 3>(buf, nb, nbm, es, bs, L, n, mm, nbfm, skip_mid, tw);
+      if constexpr (BFAST) {
+        if (r == 4) dit_stage<R, SIGN, BFAST, 4>(buf, nb, nbm, es, bs, L, n, mm, nbfm, false, tw);
+        else if (r == 2) dit_stage<R, SIGN, BFAST, 2>(buf, nb, nbm, es, bs, L, n, mm, nbfm, false, tw);
+        else dit_stage<R, SIGN, BFAST, 3>(buf, nb, nbm, es, bs, L, n, mm, nbfm, skip_mid, tw);
+      } else {  // the x transforms: es = 1, padded buffer
+        if (r == 4) dit_stage_padded<R, SIGN, 4>(buf, nb, bs, L, n, mm, nbfm, false, tw);
+        else if (r == 2) dit_stage_padded<R, SIGN, 2>(buf, nb, bs, L, n, mm, nbfm, false, tw);
+        else dit_stage_padded<R, SIGN, 3>(buf, nb, bs, L, n, mm, nbfm, skip_mid, tw);
+      }
       __syncthreads();
     }
   } else {

@@ -143,13 +143,13 @@ __device__ void x_inverse(const cpx_t<R>* const* rows, int nr, cpx_t<R>* F, int 
     const double2 w = rtw[k];
     const R wr = (R)w.x, wi = (R)-w.y;  // exp(+2 pi i k/n)
     const T2 q = T2{wr * df.x - wi * df.y, wr * df.y + wi * df.x};
-    F[r * hp + ph.perm[k]] = T2{s.x - q.y, s.y + q.x};
+    F[sxi<R>(r * hp + ph.perm[k])] = T2{s.x - q.y, s.y + q.x};
   }
   __syncthreads();
   fft_dit<R, +1, false>(F, nr, 1, hp, ph, false);
   for (int e = threadIdx.x; e < nr * h; e += blockDim.x) {
     const int r = e / h, m = e - r * h;
-    const T2 z = F[r * hp + m];
+    const T2 z = F[sxi<R>(r * hp + m)];
     out[r][2 * m] = z.x;
     out[r][2 * m + 1] = z.y;
   }
@@ -168,9 +168,9 @@ __device__ void x_forward_packed(int nr, cpx_t<R>* F, int hp, cpx_t<R>* const* r
   fft_dit<R, -1, false>(F, nr, 1, hp, ph, false);
   for (int e = threadIdx.x; e < nr * nkx; e += blockDim.x) {
     const int r = e / nkx, k = e - r * nkx;
-    const T2 zk = F[r * hp + k];
+    const T2 zk = F[sxi<R>(r * hp + k)];
     const int k2 = (h - k) % h;
-    T2 zc = F[r * hp + k2];
+    T2 zc = F[sxi<R>(r * hp + k2)];
     zc.y = -zc.y;
     const T2 E = T2{(R)0.5 * (zk.x + zc.x), (R)0.5 * (zk.y + zc.y)};
     const T2 D = csub(zk, zc);
@@ -207,12 +207,12 @@ __device__ void x_inverse_pair(const cpx_t<R>* rowA, const cpx_t<R>* rowB, cpx_t
       const T2 a = rowA[n - k], b = rowB[n - k];
       z = T2{a.x + b.y, b.x - a.y};
     }
-    F[pf.perm[k]] = z;
+    F[sxi<R>(pf.perm[k])] = z;
   }
   __syncthreads();
   fft_dit<R, +1, false>(F, 1, 1, n, pf, false);
   for (int x = threadIdx.x; x < n; x += blockDim.x) {
-    const T2 z = F[x];
+    const T2 z = F[sxi<R>(x)];
     outA[x] = z.x;
     outB[x] = z.y;
   }
@@ -229,8 +229,8 @@ __device__ void x_forward_pairs(int np2, cpx_t<R>* F, cpx_t<R>* const* rows, con
   fft_dit<R, -1, false>(F, np2, 1, n, pf, false);
   for (int e = threadIdx.x; e < np2 * nkx; e += blockDim.x) {
     const int p = e / nkx, k = e - p * nkx;
-    const T2 zk = F[p * n + k];
-    const T2 zc = F[p * n + ((n - k) % n)];
+    const T2 zk = F[sxi<R>(p * n + k)];
+    const T2 zc = F[sxi<R>(p * n + ((n - k) % n))];
     rows[2 * p][k] = T2{sc * (zk.x + zc.x), sc * (zk.y - zc.y)};
     rows[2 * p + 1][k] = T2{sc * (zk.y + zc.y), sc * (zc.x - zk.x)};
   }
@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ngx = d.ngx, h = ngx / 2, hp = h + 1;
   T2* F = reinterpret_cast<T2*>(smraw);             // 3 vectors of ngx (also holds the half-length v transform)
-  R* rowsm = reinterpret_cast<R*>(F + 3 * ngx);     // 6 rows of ngx
+  R* rowsm = reinterpret_cast<R*>(F + sx_elems<R>(3 * (size_t)ngx));  // 6 rows of ngx
   R* up = rowsm;
   R* wp = rowsm + ngx;
   R* vp = rowsm + 2 * ngx;
@@ -294,8 +294,8 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
       const int px = pf.perm[x];
       if (cprod) {
         const R v = vp[x] + wcj * (vc[x] - vp[x]);
-        F[px] = T2{u * u, u * w};
-        F[ngx + px] = T2{w * w, v * v};
+        F[sxi<R>(px)] = T2{u * u, u * w};
+        F[sxi<R>(ngx + px)] = T2{w * w, v * v};
         if (a.want_cfl) {
           const double cv = fabs((double)u) * a.dxi + fabs((double)v) * dyi + fabs((double)w) * a.dzi;
           cmax = fmax(cmax, cv);
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
       if (fprod) {
         const R uf = up[x] + wfj * (u - up[x]);
         const R wf = wp[x] + wfj * (w - wp[x]);
-        F[fslot * ngx + px] = T2{uf * vp[x], wf * vp[x]};
+        F[sxi<R>(fslot * ngx + px)] = T2{uf * vp[x], wf * vp[x]};
       }
     }
     __syncthreads();
@@ -347,7 +347,7 @@ void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const 
   const int nlev = L1 - L0 + 1;
   if (nlev <= 0) return;
   dim3 grid(d.ngz, (nlev + a.chunk - 1) / a.chunk);
-  size_t sm = sizeof(cpx_t<R>) * 3 * (size_t)d.ngx + sizeof(R) * 6 * (size_t)d.ngx;
+  size_t sm = sizeof(cpx_t<R>) * sx_elems<R>(3 * (size_t)d.ngx) + sizeof(R) * 6 * (size_t)d.ngx;
   k_xprod<R><<<grid, 256, sm, st>>>(a, d, ph, pf, rtw);
 }
 
@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(128) k_xmask(MaskArgs<R> a, Dims d, FftPlan ph
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ngx = d.ngx, h = ngx / 2, hp = h + 1;
   T2* F = reinterpret_cast<T2*>(smraw);
-  R* rr = reinterpret_cast<R*>(F + 2 * hp);
+  R* rr = reinterpret_cast<R*>(F + sx_elems<R>(2 * (size_t)hp));
   R* ll = rr + ngx;
   const int kz = blockIdx.x;
   int pl = blockIdx.y, f = 0;
@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(128) k_xmask(MaskArgs<R> a, Dims d, FftPlan ph
       v[e] = rr[x];
       if (msk[x]) v[e] = (tip >= 0) ? mb * ll[x] : (R)0;
     }
-    F[ph.perm[m]] = T2{v[0], v[1]};
+    F[sxi<R>(ph.perm[m])] = T2{v[0], v[1]};
   }
   __syncthreads();
   T2* rows[1] = {row};
@@ -403,7 +403,7 @@ void launch_xmask(const MaskArgs<R>& a, const Dims& d, const FftPlan& ph, const 
   if (tot == 0) return;
   dim3 grid(d.ngz, tot);
   const int hp = d.ngx / 2 + 1;
-  size_t sm = sizeof(cpx_t<R>) * 2 * (size_t)hp + sizeof(R) * 2 * (size_t)d.ngx;
+  size_t sm = sizeof(cpx_t<R>) * sx_elems<R>(2 * (size_t)hp) + sizeof(R) * 2 * (size_t)d.ngx;
   k_xmask<R><<<grid, 128, sm, st>>>(a, d, ph, rtw);
 }
 
