@@ -204,6 +204,13 @@ int lh_profile_step(lh_handle* h, double* ms_by_kind, int32_t* count_by_kind, in
  * captured with the new shapes. */
 int lh_autotune(lh_handle* h, int32_t* tx, int32_t* chunk);
 
+/* The launch shapes the next step uses (no reference counterpart): z tile
+ * width, levels per product-pass CTA, and whether the product pass transforms
+ * the face pair after the centre pairs through a smaller buffer (1) or all
+ * three pairs at once (0); lh_autotune picks that by timing too.  Any pointer
+ * may be NULL. */
+int lh_get_launch_shapes(lh_handle* h, int32_t* tx, int32_t* chunk, int32_t* xsplit);
+
 
 /* Divergence-free projection (solveP + v_corr with kRK = 1, the operation of
  * lh_project) of caller-owned device arrays u1, u2, u3 (plane layout), for

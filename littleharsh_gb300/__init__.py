@@ -32,7 +32,7 @@ EXPORTED_SYMBOLS = [
     "lh_cfl_dt", "lh_project", "lh_spectra_accumulate", "lh_spectra_flush", "lh_stats_accumulate",
     "lh_stats_flush", "lh_cond_accumulate", "lh_cond_flush", "lh_last_step_ms", "lh_profile_step",
     "lh_project_noalloc", "lh_ensemble_create", "lh_ensemble_step", "lh_ensemble_last_error",
-    "lh_ensemble_free", "lh_autotune", "lh_write_restart", "lh_read_restart", "lh_write_stats", "lh_write_spectra", "lh_read_input", "lh_setup_grid", "lh_setup_canopy",
+    "lh_ensemble_free", "lh_autotune", "lh_get_launch_shapes", "lh_write_restart", "lh_read_restart", "lh_write_stats", "lh_write_spectra", "lh_read_input", "lh_setup_grid", "lh_setup_canopy",
     # include/lh_srnet.h: kernels of the learned warm start
     "lh_sr_conv_fwd", "lh_sr_conv_fwd_tc", "lh_sr_tc_status", "lh_sr_conv_wgrad", "lh_sr_flip_weights", "lh_sr_mse", "lh_sr_adam",
 ]
@@ -117,6 +117,7 @@ def load_library(build: bool = True) -> C.CDLL:
     L.lh_last_step_ms.argtypes = [vp, _dp, C.POINTER(i32)]
     L.lh_profile_step.argtypes = [vp, _dp, C.c_void_p, i32]
     L.lh_autotune.argtypes = [vp, C.POINTER(i32), C.POINTER(i32)]
+    L.lh_get_launch_shapes.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]
     L.lh_project_noalloc.argtypes = [C.POINTER(Params)] + [_dp] * 3 + [C.c_void_p] * 3 + [C.c_double, C.c_void_p]
     L.lh_write_restart.argtypes = [vp, C.POINTER(Params), _dp, _dp, cp, cp, i32]
     L.lh_read_restart.argtypes = [vp, cp, cp, _dp, C.POINTER(i32)]
@@ -331,10 +332,16 @@ class Solver:
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNEL_KINDS)}
 
     def autotune(self) -> dict:
-        """Pick the z tile width and the product pass's levels per CTA by timing (lh_autotune)."""
-        tx, ch = C.c_int32(0), C.c_int32(0)
-        self._check(load_library().lh_autotune(self.h, C.byref(tx), C.byref(ch)))
-        return {"tx": tx.value, "chunk": ch.value}
+        """Pick the z tile width, the product pass's levels per CTA and its buffer split by timing
+        (lh_autotune); returns the shapes the next step uses."""
+        self._check(load_library().lh_autotune(self.h, None, None))
+        return self.launch_shapes()
+
+    def launch_shapes(self) -> dict:
+        """The z tile width, levels per product-pass CTA and product-pass buffer split in use."""
+        tx, ch, xs = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+        self._check(load_library().lh_get_launch_shapes(self.h, C.byref(tx), C.byref(ch), C.byref(xs)))
+        return {"tx": tx.value, "chunk": ch.value, "xsplit": xs.value}
 
     # diagnostics ------------------------------------------------------------
     def divmax(self) -> float:

@@ -80,6 +80,7 @@ struct lh_handle {
   double2* rtw2 = nullptr;
   Dims dmid{};              // the middle band's plane geometry (bands only)
   int tx = 8, chunk = 16;
+  int xsplit = 0;  // x-pass: face pair transformed on its own (smaller shared-memory footprint)
   // state
   double t_now = 0, dt = 0;
   bool have_fields = false, have_dt = false;
@@ -372,7 +373,7 @@ void enqueue_nonlinear(lh_handle* h, cudaStream_t st, bool zinv, bool xprod, boo
       for (int i = 0; i < 6; ++i) a.out[i] = (T2*)h->mixp[i];
       a.wc = h->t.wc; a.wf = h->t.wf; a.dyc = h->t.dyc;
       a.dxi = db.ngx / h->Lx; a.dzi = db.ngz / h->Lz;
-      a.sc = h->sc; a.want_cfl = 0; a.chunk = h->chunk;
+      a.sc = h->sc; a.want_cfl = 0; a.chunk = h->chunk; a.split = h->xsplit;
       a.c_lo = B.c_lo; a.c_hi = B.c_hi; a.f_lo = B.f_lo; a.f_hi = B.f_hi;
       launch_xprod<R>(a, db, *B.ph, *B.pf, B.rtw, st);
       mark(h, K_XPROD);
@@ -844,6 +845,7 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
   // launch-shape overrides for tuning sweeps: LH_TX (z tile width, 1..64), LH_CHUNK (levels per x-pass CTA)
   if (const char* v = std::getenv("LH_TX")) { const int x = std::atoi(v); if (x >= 1 && x <= 64) h->tx = x; }
   if (const char* v = std::getenv("LH_CHUNK")) { const int x = std::atoi(v); if (x >= 1 && x <= 4096) h->chunk = x; }
+  if (const char* v = std::getenv("LH_XSPLIT")) h->xsplit = std::atoi(v) != 0 ? 1 : 0;
   {
     const cudaError_t e = configure_kernels();
     if (e != cudaSuccess) return bail(fail(h, LH_ECUDA, "kernel attributes: %s", cudaGetErrorString(e)));
@@ -1181,6 +1183,19 @@ int lh_autotune(lh_handle* h, int32_t* tx_out, int32_t* chunk_out) {
     if (ms < best) { best = ms; best_ch = ch; }
   }
   h->chunk = best_ch;
+  // the x pass with the face pair transformed on its own: fewer buffer vectors, more CTAs per SM
+  {
+    const int xs0 = h->xsplit;
+    float t2[2] = {0.f, 0.f};
+    for (int xs = 0; xs < 2; ++xs) {
+      h->xsplit = xs;
+      t2[xs] = h->precision == LH_PREC_MIXED ? time_parts<float>(h, false, true, e0, e1)
+                                             : time_parts<double>(h, false, true, e0, e1);
+      if (t2[xs] < 0.f) { h->xsplit = xs0; cudaEventDestroy(e0); cudaEventDestroy(e1); return fail(h, LH_ECUDA, "autotune: product pass failed"); }
+    }
+    h->xsplit = t2[1] < t2[0] ? 1 : 0;
+    if (h->xsplit != xs0 && h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; ++h->graph_gen; }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   CU(h, cudaGetLastError());
@@ -1190,6 +1205,14 @@ int lh_autotune(lh_handle* h, int32_t* tx_out, int32_t* chunk_out) {
   }
   if (tx_out) *tx_out = h->tx;
   if (chunk_out) *chunk_out = h->chunk;
+  return LH_OK;
+}
+
+int lh_get_launch_shapes(lh_handle* h, int32_t* tx, int32_t* chunk, int32_t* xsplit) {
+  if (!h) return LH_EINVAL;
+  if (tx) *tx = h->tx;
+  if (chunk) *chunk = h->chunk;
+  if (xsplit) *xsplit = h->xsplit;
   return LH_OK;
 }
 
@@ -1268,7 +1291,7 @@ int lh_cfl_dt(lh_handle* h, double cfl, double* dt_out) {
       for (int i = 0; i < 6; ++i) a.out[i] = (T2*)h->mixp[i];
       a.wc = h->t.wc; a.wf = h->t.wf; a.dyc = h->t.dyc;
       a.dxi = db.ngx / h->Lx; a.dzi = db.ngz / h->Lz;
-      a.sc = h->sc; a.want_cfl = 1; a.chunk = h->chunk;
+      a.sc = h->sc; a.want_cfl = 1; a.chunk = h->chunk; a.split = h->xsplit;
       a.c_lo = B.c_lo; a.c_hi = B.c_hi; a.f_lo = B.c_lo; a.f_hi = B.c_lo - 1;  // centres only
       launch_xprod<R>(a, db, *B.ph, *B.pf, B.rtw, h->st);
     }

@@ -138,6 +138,7 @@ struct ProdArgs {
   DevScalars* sc;       // CFL maximum accumulated here when want_cfl
   int want_cfl;
   int chunk;
+  int split;            // 1: the face pair is transformed after the centre pairs, through two buffer vectors
   // levels this launch forms products on (a band's planes): centres c_lo..c_hi, faces f_lo..f_hi
   int c_lo, c_hi, f_lo, f_hi;
 };

@@ -243,8 +243,9 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
   using T2 = cpx_t<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ngx = d.ngx, h = ngx / 2, hp = h + 1;
-  T2* F = reinterpret_cast<T2*>(smraw);             // 3 vectors of ngx (also holds the half-length v transform)
-  R* rowsm = reinterpret_cast<R*>(F + sx_elems<R>(3 * (size_t)ngx));  // 6 rows of ngx
+  // 3 vectors of ngx, 2 with a.split (also holds the half-length v transform)
+  T2* F = reinterpret_cast<T2*>(smraw);
+  R* rowsm = reinterpret_cast<R*>(F + sx_elems<R>((a.split ? 2 : 3) * (size_t)ngx));  // 6 rows of ngx
   R* up = rowsm;
   R* wp = rowsm + ngx;
   R* vp = rowsm + 2 * ngx;
@@ -287,8 +288,15 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
     const R wcj = (R)a.wc[jj];
     const R wfj = fprod ? (R)a.wf[jj - 1] : (R)0;
     const double dyi = a.dyc[jj];
-    // pairs: (uu, uw), (ww, vv) at centre jj; (uv, vw) at face jj-1 (after the centre pairs, or first)
-    const int fslot = cprod ? 2 : 0;
+    // pairs: (uu, uw), (ww, vv) at centre jj; (uv, vw) at face jj-1 (after the centre pairs, or first);
+    // with a.split and both kinds, the face pair goes through the buffer after the centre pairs' transform
+    const bool later = a.split && cprod && fprod;
+    const int fslot = (cprod && !later) ? 2 : 0;
+    auto face_pair = [&](int x, R u, R w, int px) {
+      const R uf = up[x] + wfj * (u - up[x]);
+      const R wf = wp[x] + wfj * (w - wp[x]);
+      F[sxi<R>(fslot * ngx + px)] = T2{uf * vp[x], wf * vp[x]};
+    };
     for (int x = threadIdx.x; x < ngx; x += blockDim.x) {
       const R u = uc[x], w = wc[x];
       const int px = pf.perm[x];
@@ -301,11 +309,7 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
           cmax = fmax(cmax, cv);
         }
       }
-      if (fprod) {
-        const R uf = up[x] + wfj * (u - up[x]);
-        const R wf = wp[x] + wfj * (w - wp[x]);
-        F[sxi<R>(fslot * ngx + px)] = T2{uf * vp[x], wf * vp[x]};
-      }
+      if (fprod && !later) face_pair(x, u, w, px);
     }
     __syncthreads();
     if (cprod || fprod) {
@@ -320,7 +324,14 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
         rows[2 * npair + 1] = a.out[5] + (size_t)(jj - 1) * d.mp + rowoff;
         ++npair;
       }
-      x_forward_pairs<R>(npair, F, rows, d, pf);
+      if (later) {
+        x_forward_pairs<R>(2, F, rows, d, pf);
+        for (int x = threadIdx.x; x < ngx; x += blockDim.x) face_pair(x, uc[x], wc[x], pf.perm[x]);
+        __syncthreads();
+        x_forward_pairs<R>(1, F, rows + 4, d, pf);
+      } else {
+        x_forward_pairs<R>(npair, F, rows, d, pf);
+      }
     }
     // current becomes previous
     R* t;
@@ -347,7 +358,7 @@ void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const 
   const int nlev = L1 - L0 + 1;
   if (nlev <= 0) return;
   dim3 grid(d.ngz, (nlev + a.chunk - 1) / a.chunk);
-  size_t sm = sizeof(cpx_t<R>) * sx_elems<R>(3 * (size_t)d.ngx) + sizeof(R) * 6 * (size_t)d.ngx;
+  size_t sm = sizeof(cpx_t<R>) * sx_elems<R>((a.split ? 2 : 3) * (size_t)d.ngx) + sizeof(R) * 6 * (size_t)d.ngx;
   k_xprod<R><<<grid, 256, sm, st>>>(a, d, ph, pf, rtw);
 }
 

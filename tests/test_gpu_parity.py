@@ -176,6 +176,26 @@ def test_autotune_keeps_results(oracle_mod):
         np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_split_face_pair_keeps_results(oracle_mod, monkeypatch, mixed):
+    """The x pass that transforms the face pair after the centre pairs (two buffer vectors instead of
+    three) runs the same transforms one vector at a time: bit for bit the same step."""
+    import littleharsh_gb300 as lh
+    o, s0 = _pair(oracle_mod, C1)
+    prec = lh.PREC_MIXED if mixed else lh.PREC_FP64
+    sols = []
+    for split in ("0", "1"):
+        monkeypatch.setenv("LH_XSPLIT", split)
+        s = lh.Solver(lh.Config(**C1), precision=prec)
+        s.set_fields(*s0.get_fields())
+        tm = s0.time()
+        s.set_time(0.0, tm["dt"], 0.0, tm["QxT"])
+        s.step(3)
+        sols.append(s)
+    for a, b in zip(sols[0].get_fields(), sols[1].get_fields()):
+        np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("cfg", [SMALL, C1], ids=["canopy24", "config1_96x97"])
 def test_broadband_field(oracle_mod, cfg):
     """Every mode populated (not only |k| <= 8): the high modes, the 3/2 truncation and the Nyquist
