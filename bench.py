@@ -31,13 +31,14 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-from littleharsh_gb300.workloads import CONFIG1, CONFIG2, CONFIG2_BANDS, MID288, ensemble_configs  # noqa: E402
+from littleharsh_gb300.workloads import CONFIG1, CONFIG2, CONFIG2_BANDS, MID288, XZ576_NY49, ensemble_configs  # noqa: E402
 
 WORKLOADS = {
     "config2_576x576x450_fp64": CONFIG2,
     "config2_bands_576_384x450_fp64": CONFIG2_BANDS,
     "config1_96x96x130_fp64": CONFIG1,
     "mid_288x288x226_fp64": MID288,
+    "xz576_ny49_fp64": XZ576_NY49,
 }
 DEFAULT_WORKLOAD = "config2_576x576x450_fp64"
 METRIC = "grid-pt RK3 steps/s"

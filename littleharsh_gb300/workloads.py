@@ -25,6 +25,10 @@ CONFIG2_BANDS = dict(CONFIG2, ngalx2=384, ngalz2=384)
 MID288 = dict(Re=5000.0, alp=1.0, bet=2.0, ngalx=288, ngalz=288, ny=193, dyq=13.6, ppp=5, geometry_type=3, posth=0.1,
               dsty=16, dstx=4, dstz=4, ntilex=24, ntilez=12, flag_ctpress=0)
 
+# capture case for the profiler: configuration 2's x and z lengths (the same transform lengths and shared-memory
+# footprints per CTA) on 49 y points (58 u levels), ~2.5 GB on the device, x-pass inputs ~5x the L2
+XZ576_NY49 = dict(CONFIG2, ny=49, dsty=4)
+
 # configuration 1 at half the resolution in x, z and y: the coarse grid of the
 # learned warm start on configuration 1's geometry (posts 1 x 2 points)
 CONFIG1_COARSE = dict(CONFIG1, ngalx=48, ngalz=48, ny=49, dsty=8, dstx=1, dstz=2)
