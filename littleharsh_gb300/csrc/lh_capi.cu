@@ -544,8 +544,9 @@ int read_scalars(lh_handle* h, DevScalars* out) {
 int host_flowrate(lh_handle* h, double* Q) {
   const Dims& d = h->d;
   std::vector<double2> col(d.nn + 2);
-  for (int j = 0; j <= d.nn + 1; ++j)
-    CU(h, cudaMemcpyAsync(&col[j], h->u1 + (size_t)(j - d.ju0) * d.np, sizeof(double2), cudaMemcpyDeviceToHost, h->st));
+  // the (0,0) mode of levels 0..nn+1, gathered on the device into scratch and read back in one copy
+  launch_gather_col(h->u1 + (size_t)(0 - d.ju0) * d.np, d.np, d.nn + 2, h->stage, h->st);
+  CU(h, cudaMemcpyAsync(col.data(), h->stage, sizeof(double2) * (d.nn + 2), cudaMemcpyDeviceToHost, h->st));
   CU(h, cudaStreamSynchronize(h->st));
   double q = 0.0;
   for (int j = 1; j <= d.nn + 1; ++j) q = q + (h->yv[j - d.ju0] - h->yv[j - 1 - d.ju0]) * col[j].x;

@@ -182,6 +182,8 @@ void launch_divergence(const double2* u1, const double2* u2, const double2* u3, 
                        const Tables& t, cudaStream_t st);
 void launch_absmax(const double2* x, size_t n, DevScalars* sc, cudaStream_t st);
 void launch_transpose(const double2* src, double2* dst, int rows, int cols, cudaStream_t st);
+// dst[j] = src[j * stride], j < n (one strided column gathered into contiguous scratch)
+void launch_gather_col(const double2* src, size_t stride, int n, double2* dst, cudaStream_t st);
 void launch_spectra(const double2* u1, const double2* u2, const double2* u3, const double2* p, double* sp,
                     const Dims& d, const Tables& t, cudaStream_t st);
 void launch_stats(const double2* u1, const double2* u2, const double2* u3, const double2* p, double2* vc,

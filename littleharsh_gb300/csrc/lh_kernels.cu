@@ -788,6 +788,15 @@ void launch_absmax(const double2* x, size_t n, DevScalars* sc, cudaStream_t st) 
 }
 
 // [rows][cols] -> [cols][rows] through a shared-memory tile.
+__global__ void k_gather_col(const double2* __restrict__ src, size_t stride, int n, double2* __restrict__ dst) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) dst[j] = src[(size_t)j * stride];
+}
+
+void launch_gather_col(const double2* src, size_t stride, int n, double2* dst, cudaStream_t st) {
+  if (n > 0) k_gather_col<<<(n + 127) / 128, 128, 0, st>>>(src, stride, n, dst);
+}
+
 __global__ void k_transpose(const double2* __restrict__ src, double2* __restrict__ dst, int rows, int cols) {
   __shared__ double2 tile[32][33];
   const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
