@@ -672,54 +672,92 @@ void launch_build_dg(double* dg2, double* dg3, const double* rows, const Dims& d
 // or one wall band of a short one).  The divergence is formed on the fly in
 // the forward sweep; the backward sweep adds psi to p and corrects u, w on the
 // same levels and v on the faces between them.
-__device__ __forceinline__ void psolve_segment(double2* u1, double2* u2, double2* u3, double2* p, double2* psi,
-                                               const Dims& d, const Tables& t, int col, double kx, double kz,
-                                               double dtirk, double dtrk, int lo, int hi, bool pin00) {
+__device__ __forceinline__ void psolve_segment(double2* __restrict__ u1, double2* __restrict__ u2,
+                                               double2* __restrict__ u3, double2* __restrict__ p,
+                                               double2* __restrict__ psi, const Dims& d, const Tables& t, int col,
+                                               double kx, double kz, double dtirk, double dtrk, int lo, int hi,
+                                               bool pin00) {
+  // levels are loaded four at a time ahead of the recurrences (the arithmetic and its order are those of
+  // one level at a time)
   const size_t np = d.np;
+  const double* __restrict__ dg2 = t.dg2;
+  const double* __restrict__ dg3 = t.dg3;
   double2 x = double2{0.0, 0.0};
-  for (int jp = lo; jp <= hi; ++jp) {
-    const int ju = jp + 1;
-    const double2 a = u1[(size_t)ju * np + col], w = u3[(size_t)ju * np + col];
-    const double2 v1 = u2[(size_t)ju * np + col], v0 = u2[(size_t)jp * np + col];
-    const double c = t.cu[ju];
-    double2 dv = double2{(-kx * a.y - kz * w.y) + c * (v1.x - v0.x), (kx * a.x + kz * w.x) + c * (v1.y - v0.y)};
+  double2 vlo = u2[(size_t)lo * np + col];  // v on face jp, carried from the level below
+  auto fwd = [&](int jp, const double2& a, const double2& w, const double2& v1, const double2& v0, double b2) {
+    const double c = t.cu[jp + 1];
+    const double2 dv = double2{(-kx * a.y - kz * w.y) + c * (v1.x - v0.x), (kx * a.x + kz * w.x) + c * (v1.y - v0.y)};
     double2 ps = double2{dtirk * dv.x, dtirk * dv.y};
     if (pin00 && jp == lo) ps = double2{0.0, 0.0};
-    const double b2 = t.dg2[(size_t)jp * np + col];
     if (jp == lo) x = double2{ps.x * b2, ps.y * b2};
     else {
       const double b1 = t.dg1[jp];
       x = double2{(ps.x - b1 * x.x) * b2, (ps.y - b1 * x.y) * b2};
     }
     psi[(size_t)jp * np + col] = x;
+  };
+  int jp = lo;
+  for (; jp + 3 <= hi; jp += 4) {
+    double2 A[4], W[4], V[4];
+    double B2[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const size_t cu = (size_t)(jp + q + 1) * np + col;
+      A[q] = u1[cu];
+      W[q] = u3[cu];
+      V[q] = u2[cu];
+      B2[q] = dg2[(size_t)(jp + q) * np + col];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) fwd(jp + q, A[q], W[q], V[q], q == 0 ? vlo : V[q - 1], B2[q]);
+    vlo = V[3];
+  }
+  for (; jp <= hi; ++jp) {
+    const size_t cu = (size_t)(jp + 1) * np + col;
+    const double2 v1 = u2[cu];
+    fwd(jp, u1[cu], u3[cu], v1, vlo, dg2[(size_t)jp * np + col]);
+    vlo = v1;
   }
   const double kxd = dtrk * kx, kzd = dtrk * kz;
   double2 xn = x;  // psi(hi)
-  for (int jp = hi; jp >= lo; --jp) {
-    double2 xc;
-    if (jp == hi) xc = xn;
-    else {
-      const double2 v = psi[(size_t)jp * np + col];
-      const double b3 = t.dg3[(size_t)jp * np + col];
-      xc = double2{v.x - b3 * xn.x, v.y - b3 * xn.y};
-    }
-    const size_t cp = (size_t)jp * np + col, cu = (size_t)(jp + 1) * np + col;
-    double2 pp = p[cp];
+  auto bwd = [&](int jq, const double2& v, double b3, const double2& pp, const double2& a, const double2& w,
+                 const double2& vv) {
+    const double2 xc = jq == hi ? xn : double2{v.x - b3 * xn.x, v.y - b3 * xn.y};
+    const size_t cp = (size_t)jq * np + col, cu = (size_t)(jq + 1) * np + col;
     p[cp] = double2{pp.x + xc.x, pp.y + xc.y};
-    double2 a = u1[cu];
     u1[cu] = double2{a.x - (-kxd * xc.y), a.y - (kxd * xc.x)};
-    double2 w = u3[cu];
     u3[cu] = double2{w.x - (-kzd * xc.y), w.y - (kzd * xc.x)};
-    if (jp < hi) {
-      const double f = dtrk * t.cv[jp + 1];
-      double2 v = u2[cu];
-      u2[cu] = double2{v.x - f * (xn.x - xc.x), v.y - f * (xn.y - xc.y)};
+    if (jq < hi) {
+      const double f = dtrk * t.cv[jq + 1];
+      u2[cu] = double2{vv.x - f * (xn.x - xc.x), vv.y - f * (xn.y - xc.y)};
     }
     xn = xc;
+  };
+  jp = hi;
+  for (; jp - 3 >= lo; jp -= 4) {
+    double2 Ps[4], P[4], A[4], W[4], V[4];
+    double B3[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int jq = jp - q;
+      const size_t cp = (size_t)jq * np + col, cu = (size_t)(jq + 1) * np + col;
+      Ps[q] = psi[cp];
+      B3[q] = dg3[cp];
+      P[q] = p[cp];
+      A[q] = u1[cu];
+      W[q] = u3[cu];
+      V[q] = u2[cu];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) bwd(jp - q, Ps[q], B3[q], P[q], A[q], W[q], V[q]);
+  }
+  for (; jp >= lo; --jp) {
+    const size_t cp = (size_t)jp * np + col, cu = (size_t)(jp + 1) * np + col;
+    bwd(jp, psi[cp], dg3[cp], p[cp], u1[cu], u3[cu], u2[cu]);
   }
 }
 
-__global__ void __launch_bounds__(128) k_psolve(double2* u1, double2* u2, double2* u3, double2* p, double2* psi,
+__global__ void __launch_bounds__(128, 4) k_psolve(double2* u1, double2* u2, double2* u3, double2* p, double2* psi,
                                                 Dims d, Tables t, double dtirk, double dtrk, double gwb,
                                                 double gwt) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
