@@ -384,6 +384,7 @@ void enqueue_nonlinear(lh_handle* h, cudaStream_t st, bool zinv, bool xprod, boo
       for (int i = 0; i < 6; ++i) {
         const int lo = i < 4 ? B.c_lo : B.f_lo, hi = i < 4 ? B.c_hi : B.f_hi;
         J.j[i] = ZJob<R>{nullptr, outs[i], (T2*)h->mixp[i] + (size_t)lo * db.mp, nullptr, lo, std::max(0, hi - lo + 1)};
+        J.j[i].out32 = sizeof(R) == 4;  // the mixed form keeps its product spectra in FP32
       }
       J.njobs = 6;
       J.maxlev = std::max(B.c_hi - B.c_lo + 1, B.f_hi - B.f_lo + 1);
@@ -422,7 +423,13 @@ int enqueue_substage(lh_handle* h, int k, int upto) {
     a.u1 = h->u1; a.u2 = h->u2; a.u3 = h->u3; a.p = h->p;
     a.n1 = h->n1; a.n2 = h->n2; a.n3 = h->n3;
     a.r1 = h->r1; a.r2 = h->r2; a.r3 = h->r3;
-    a.puu = h->puu; a.puw = h->puw; a.pww = h->pww; a.pvv = h->pvv; a.puv = h->puv; a.pvw = h->pvw;
+    {
+      const double2* pr[6] = {h->puu, h->puw, h->pww, h->pvv, h->puv, h->pvw};
+      for (int q = 0; q < 6; ++q) {
+        if (sizeof(R) == 4) a.p32[q] = reinterpret_cast<const float2*>(pr[q]);
+        else a.p64[q] = pr[q];
+      }
+    }
     a.lytip = h->lytip;
     a.tipu[0] = h->tipu[0]; a.tipu[1] = h->tipu[1]; a.tipv[0] = h->tipv[0]; a.tipv[1] = h->tipv[1];
     a.sc = h->sc;

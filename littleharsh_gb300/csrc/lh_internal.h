@@ -110,6 +110,7 @@ struct ZJob {
   cpx_t<R>* mix;            // mixed planes, contiguous per job
   const int* levels;
   int lev0, nlev;
+  int out32;                // z-forward: write FP32 spectra (cpx_t<R>) to spec_out instead of FP64
 };
 
 constexpr int kMaxJobs = 12;
@@ -162,7 +163,9 @@ struct AsmArgs {
   const double2 *u1, *u2, *u3, *p;
   double2 *n1, *n2, *n3;     // in: Nu of the previous substage, out: Nu of this one
   double2 *r1, *r2, *r3;     // out: right-hand sides divided by axz
-  const double2 *puu, *puw, *pww, *pvv, *puv, *pvw;
+  // product spectra uu, uw, ww, vv (centres), uv, vw (faces): FP64, or FP32 in the mixed form (p32 set)
+  const double2* p64[6];
+  const float2* p32[6];
   double2* lytip;            // y-Laplacian of the tip planes [6][np]
   int tipu[2], tipv[2];      // level indices of the tip planes (u grid, v grid) or -1
   const DevScalars* sc;

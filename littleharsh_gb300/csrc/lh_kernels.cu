@@ -91,8 +91,24 @@ __global__ void __launch_bounds__(256) k_zfwd(ZJobs<R> jobs, Dims d, FftPlan pz,
   // the truncation keeps slots [0, N2/2) and [Ngz - N2/2, Ngz): the middle third of the last radix-3
   // stage's output is never read when N2/2 = Ngz/3
   fft_dit<R, -1, true>(sm, nb, tx, 1, pz, pz.prune_mid != 0);
-  double2* __restrict__ dst = J.spec_out + (size_t)lev * d.np;
   const int h = d.nz / 2, gap = d.ngz - d.nz;
+  if constexpr (sizeof(R) == 4) {
+    if (J.out32) {  // the mixed form's product spectra stay FP32 (only the nonlinear term reads them)
+      T2* __restrict__ dst = reinterpret_cast<T2*>(J.spec_out) + (size_t)lev * d.np;
+      const R sc = (R)scale;
+      for (int e = threadIdx.x; e < d.nz * tx; e += blockDim.x) {
+        const int kk = e / tx, c = e - kk * tx;
+        if (c < nb) {
+          const int slot = kk < h ? kk : kk + gap;
+          const T2 v = sm[slot * tx + c];
+          const int ks = kk < h ? kk : kk - d.nz + d.snz;
+          dst[(size_t)ks * d.spitch + i0 + c] = T2{v.x * sc, v.y * sc};
+        }
+      }
+      return;
+    }
+  }
+  double2* __restrict__ dst = J.spec_out + (size_t)lev * d.np;
   for (int e = threadIdx.x; e < d.nz * tx; e += blockDim.x) {
     const int kk = e / tx, c = e - kk * tx;
     if (c < nb) {
@@ -423,7 +439,26 @@ void launch_xmask(const MaskArgs<R>& a, const Dims& d, const FftPlan& ph, const 
 // ---------------------------------------------------------------------------
 
 __device__ __forceinline__ double2 ld(const double2* p) { return __ldg(p); }
+__device__ __forceinline__ float2 ld(const float2* p) { return __ldg(p); }
 
+// product spectra q = 0..5 (uu, uw, ww, vv, uv, vw) of the assembly's precision
+template <typename P> __device__ __forceinline__ const P* prod(const AsmArgs& a, int q);
+template <> __device__ __forceinline__ const double2* prod<double2>(const AsmArgs& a, int q) { return a.p64[q]; }
+template <> __device__ __forceinline__ const float2* prod<float2>(const AsmArgs& a, int q) { return a.p32[q]; }
+
+// The nonlinear term from the product spectra: (-kx A.y - kz B.y) + c (D1.x - D0.x) and its imaginary
+// partner (d/dx, d/dz of the in-plane products, d/dy of the face products).  The mixed form's FP32
+// spectra are combined in FP32 and only the result is widened.
+__device__ __forceinline__ double2 nterm(double2 A, double2 B, double2 D1, double2 D0, double kx, double kz, double c) {
+  return double2{(-kx * A.y - kz * B.y) + c * (D1.x - D0.x), (kx * A.x + kz * B.x) + c * (D1.y - D0.y)};
+}
+__device__ __forceinline__ double2 nterm(float2 A, float2 B, float2 D1, float2 D0, double kx, double kz, double c) {
+  const float fx = (float)kx, fz = (float)kz, fc = (float)c;
+  return double2{(double)((-fx * A.y - fz * B.y) + fc * (D1.x - D0.x)),
+                 (double)((fx * A.x + fz * B.x) + fc * (D1.y - D0.y))};
+}
+
+template <typename P>
 __global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= d.np) return;
@@ -463,14 +498,14 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
       double rx = a.C1 * L_x + a.C2 * nold.x + (a.d * kf) * pc.y;
       double ry = a.C1 * L_y + a.C2 * nold.y + -(a.d * kf) * pc.x;
       if (f == 0 && col == 0) rx = rx + (-a.d * a.sc->mpgx);
-      const double2 A = ld((f == 0 ? a.puu : a.puw) + c0);
-      const double2 B = ld((f == 0 ? a.puw : a.pww) + c0);
-      const double2* D = f == 0 ? a.puv : a.pvw;
+      const P A = ld(prod<P>(a, f == 0 ? 0 : 1) + c0);
+      const P B = ld(prod<P>(a, f == 0 ? 1 : 2) + c0);
+      const P* D = prod<P>(a, f == 0 ? 4 : 5);
       // a short column's product is zero on the middle band's planes (they hold only long modes)
-      const double2 D1 = (lng || !coarse_v(d, jj)) ? ld(D + f1) : double2{0.0, 0.0};
-      const double2 D0 = (lng || !coarse_v(d, jj - 1)) ? ld(D + f0) : double2{0.0, 0.0};
-      const double nr = (-kx * A.y - kz * B.y) + c * (D1.x - D0.x);
-      const double ni = (kx * A.x + kz * B.x) + c * (D1.y - D0.y);
+      const P D1 = (lng || !coarse_v(d, jj)) ? ld(D + f1) : P{0, 0};
+      const P D0 = (lng || !coarse_v(d, jj - 1)) ? ld(D + f0) : P{0, 0};
+      const double2 N = nterm(A, B, D1, D0, kx, kz, c);
+      const double nr = N.x, ni = N.y;
       (f == 0 ? a.n1 : a.n3)[c0] = double2{nr, ni};
       rx = rx - a.g * nr;
       ry = ry - a.g * ni;
@@ -498,11 +533,11 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
       const double2 nold = a.n2[c0];
       double rx = a.C1 * L_x + a.C2 * nold.x + C3 * (p1.x - p0.x);
       double ry = a.C1 * L_y + a.C2 * nold.y + C3 * (p1.y - p0.y);
-      const double2 A = ld(a.puv + c0), B = ld(a.pvw + c0);
-      const double2 V1 = ld(a.pvv + c0 + np), V0 = ld(a.pvv + c0);
+      const P A = ld(prod<P>(a, 4) + c0), B = ld(prod<P>(a, 5) + c0);
+      const P V1 = ld(prod<P>(a, 3) + c0 + np), V0 = ld(prod<P>(a, 3) + c0);
       const double c = t.cv[jj];
-      const double nr = (-kx * A.y - kz * B.y) + c * (V1.x - V0.x);
-      const double ni = (kx * A.x + kz * B.x) + c * (V1.y - V0.y);
+      const double2 N = nterm(A, B, V1, V0, kx, kz, c);
+      const double nr = N.x, ni = N.y;
       a.n2[c0] = double2{nr, ni};
       rx = rx - a.g * nr;
       ry = ry - a.g * ni;
@@ -518,7 +553,8 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
 
 void launch_assemble(const AsmArgs& a, const Dims& d, const Tables& t, cudaStream_t st) {
   dim3 grid((d.np + 255) / 256, d.nyu);
-  k_assemble<<<grid, 256, 0, st>>>(a, d, t);
+  if (a.p32[0]) k_assemble<float2><<<grid, 256, 0, st>>>(a, d, t);
+  else k_assemble<double2><<<grid, 256, 0, st>>>(a, d, t);
 }
 
 // Thomas sweeps of one column over levels lo..hi with an LU indexed by level
