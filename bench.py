@@ -484,7 +484,7 @@ def run_srnet(args):
                      "mma.sync", "frac_of_bf16_peak": tf / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None,
                      "ms_mma_sync_forward": res[False], "ms_tcgen05_forward": res[True],
                      "tflops_tcgen05_forward": fl / (res[True] * 1e-3) / 1e12}
-        net.tcgen05 = False
+        net.tcgen05 = True
         del x, base, tgt
         torch.cuda.empty_cache()
     out["value"] = out["train_step_config1"]["tflops"]

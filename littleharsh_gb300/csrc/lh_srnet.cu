@@ -370,21 +370,33 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
 // core matrices along M are consecutive x, 10 rows apart; the A operand of tap
 // (dz, dx) is then the same layout started dz + 10 dx rows further on, so the
 // nine taps of a stage read one halo copy through their descriptors' start
-// addresses and nothing is copied twice.  Halos are fetched with cp.async into
-// a ring of four buffers, up to three stages ahead.  One thread issues a
-// stage's 9 taps x Cin/16 x 2 tcgen05.mma (K = 16 channels, bf16 operands from
-// shared memory) and commits them to the buffer's mbarrier, whose completion
-// frees the buffer for the halo four stages on.  The accumulators are
-// double-buffered in TMEM (128 columns), so a tile's epilogue (eight warps,
-// tcgen05.ld of TMEM lanes 32 (w mod 4), half w / 4) runs while the tensor
-// cores work on the next tile.  Weights rows: [tap][k chunk][cout].  Every
-// mbarrier wait is bounded.
+// addresses and nothing is copied twice.
+//
+// The CTA is warp-specialised, its roles ordered only by mbarriers:
+//   warps 0-3 (producers) fetch halos with cp.async into a ring of four
+//     buffers; once a thread's copies for a stage have landed it fences them
+//     for the tensor core and arrives on the buffer's `full` barrier (128
+//     arrivals); a buffer is refilled after the `empty` barrier says the MMAs
+//     that read it completed;
+//   warp 8 (one thread) waits on `full`, issues the stage's 9 taps x Cin/16 x 2
+//     tcgen05.mma (K = 16 channels, bf16 operands from shared memory) into the
+//     tile's accumulator set and commits them to `empty` (and, after a tile's
+//     last stage, to the set's `acc_full`);
+//   warps 4-7 (epilogue) wait on `acc_full`, read TMEM lanes 32 (w mod 4) of
+//     both halves with tcgen05.ld, apply bias / ReLU / gate / residual, store,
+//     and arrive on `acc_empty`, which frees the set for the tile after next.
+// Two accumulator sets (128 TMEM columns) let the epilogue of one tile run
+// under the MMAs of the next.  Every wait is bounded; a wait that runs out
+// raises a shared abort flag that ends every role's loop, and the kernel
+// reports it through its error word after draining its copies and MMAs.
 constexpr int TC_TZ = 8;                     // z rows per tile
 constexpr int TC_ZR = TC_TZ + 2;             // halo z rows
 constexpr int TC_XR = TX + 2;                // halo x voxels
 constexpr int TC_HALO = TC_ZR * TC_XR;       // 16-byte rows per k-chunk plane of a halo
 constexpr int TC_NBUF = 4;                   // halo ring
-constexpr int TC_THREADS = 256;
+constexpr int TC_PRODUCERS = 128;            // warps 0-3
+constexpr int TC_THREADS = 288;              // + epilogue warps 4-7 + MMA warp 8
+constexpr int TC_MMA_WARP = 8;
 constexpr unsigned kTcSpinLimit = 1u << 20;  // bound of every mbarrier wait
 
 __device__ __forceinline__ uint64_t tc_smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
@@ -399,16 +411,22 @@ __host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-// bounded wait for the phase of parity `parity` of an mbarrier; false if it ran out
-__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity) {
+// bounded wait for the phase of parity `parity` of an mbarrier; gives up early once *abort is set; false if
+// the phase did not complete (and then raises *abort)
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, volatile int* abort) {
   uint32_t done = 0;
   for (unsigned it = 0; it < kTcSpinLimit && !done; ++it) {
     asm volatile(
         "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
         : "r"(smem_u32(bar)), "r"(parity));
+    if (!done && (it & 63) == 63 && *abort) break;
   }
+  if (!done) *abort = 1;
   return done != 0;
+}
+__device__ __forceinline__ void tc_arrive(uint64_t* bar) {
+  asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_u32(bar)) : "memory");
 }
 
 template <int CIN, int COUT, typename OutT>
@@ -424,45 +442,65 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint4* sA = reinterpret_cast<uint4*>(smem_raw);   // [TC_NBUF][KC][TC_XR][TC_ZR]
   uint4* sB = sA + (size_t)TC_NBUF * BUF;           // [27][KC][COUT]
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sB + (size_t)27 * KC * COUT);  // one per halo buffer
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + TC_NBUF);
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + (size_t)27 * KC * COUT);
+  uint64_t* empty = full + TC_NBUF;
+  uint64_t* acc_full = empty + TC_NBUF;
+  uint64_t* acc_empty = acc_full + 2;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+  volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
   for (int c = threadIdx.x; c < 27 * COUT * KC; c += blockDim.x) {  // weights -> [27][KC][COUT] rows
     const int kc = c % KC, n = (c / KC) % COUT, tap = c / (KC * COUT);
     cp_async16(sB + ((size_t)tap * KC + kc) * COUT + n, w + ((size_t)tap * COUT + n) * CIN + kc * 8, true);
   }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
   if (threadIdx.x == 0) {
-    for (int b = 0; b < TC_NBUF; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar + b)));
+    for (int b = 0; b < TC_NBUF; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(full + b)), "r"(TC_PRODUCERS));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(empty + b)));
+    }
+    for (int a = 0; a < 2; ++a) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(acc_full + a)));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(smem_u32(acc_empty + a)));
+    }
+    *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == TC_MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;\n" ::"r"(smem_u32(tslot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
   }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");           // this thread's weight copies
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");    // -> visible to the tensor core
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = *tslot;
-  const uint32_t idesc = tc_idesc(128, COUT);
 
   const int ntx = v.X / TX, ntz = v.Z / TC_TZ;
   const int ntiles = v.Y * ntz * ntx;
   const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
   const int nstages = 3 * my_tiles;
 
-  // the halo of stage st = (tile blockIdx.x + (st / 3) gridDim.x, dy = st % 3) into buffer st % TC_NBUF:
-  // rows [k chunk][x + 1][z + 1], x = -1 .. 32, z = -1 .. 8, periodic in x and z, zero outside y;
-  // every call commits one cp.async group (an empty one past the last stage)
-  auto fetch = [&](int st) {
-    if (st < nstages) {
-      const int tile = blockIdx.x + (st / 3) * gridDim.x, dy = st % 3;
+  if (warp < 4) {
+    // ---- producers: stage st = (tile blockIdx.x + (st / 3) gridDim.x, dy = st % 3) into buffer st % NBUF:
+    // rows [k chunk][x + 1][z + 1], x = -1 .. 32, z = -1 .. 8, periodic in x and z, zero outside y
+    const int p = threadIdx.x;
+    auto land = [&](int st) {  // this thread's copies of stage st have landed: hand them to the tensor core
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      tc_arrive(full + st % TC_NBUF);
+    };
+    int s = 0;
+    for (; s < nstages; ++s) {
+      if (s >= TC_NBUF && !tc_wait(empty + s % TC_NBUF, (uint32_t)((s / TC_NBUF - 1) & 1), abort)) break;
+      const int tile = blockIdx.x + (s / 3) * gridDim.x, dy = s % 3;
       const int xt = tile % ntx, rest = tile / ntx, zt = rest % ntz, y = rest / ntz;
       const int x0 = xt * TX, z0 = zt * TC_TZ;
       const int gy = y + dy - 1;
       const bool ok = gy >= 0 && gy < v.Y;
-      uint4* buf = sA + (size_t)(st % TC_NBUF) * BUF;
-      for (int c = threadIdx.x; c < TC_HALO * KC; c += blockDim.x) {
+      uint4* buf = sA + (size_t)(s % TC_NBUF) * BUF;
+      for (int c = p; c < TC_HALO * KC; c += TC_PRODUCERS) {
         const int kc = c % KC, u = c / KC;
         const int xh = u % TC_XR, zz = u / TC_XR;
         int gz = z0 + zz - 1, gx = x0 + xh - 1;
@@ -471,117 +509,126 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const size_t vox = ok ? ((size_t)gy * v.Z + gz) * v.X + gx : 0;
         cp_async16(buf + ((size_t)kc * TC_XR + xh) * TC_ZR + zz, in + vox * CIN + kc * 8, ok);
       }
-    }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-  };
-
-  // the epilogue of this CTA's tile ti from accumulator set ti % 2: warp w reads TMEM lanes
-  // 32 (w mod 4) .. +31 of half w / 4; lane m of half h is the voxel x = 16 h + m / 8, z = m mod 8
-  auto epilogue = [&](int ti) {
-    const int tile = blockIdx.x + ti * gridDim.x;
-    const int xt = tile % ntx, rest = tile / ntx, zt = rest % ntz, y = rest / ntz;
-    const int g = warp & 3, h = warp >> 2;
-    uint32_t r[32];
-    const uint32_t taddr = tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)((ti & 1) * 64 + h * 32);
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-          "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
-          "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
-          "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-    const int m = g * 32 + lane;
-    const size_t vox = ((size_t)y * v.Z + zt * TC_TZ + (m & 7)) * v.X + xt * TX + 16 * h + (m >> 3);
-#pragma unroll
-    for (int n = 0; n < COUT; n += 2) {
-      float r0 = __uint_as_float(r[n]), r1 = __uint_as_float(r[n + 1]);
-      if (epi & EPI_BIAS) { r0 += bias[n]; r1 += bias[n + 1]; }
-      if (epi & EPI_RELU) { r0 = fmaxf(r0, 0.f); r1 = fmaxf(r1, 0.f); }
-      if (epi & EPI_GATE) {
-        const __nv_bfloat162 gv = *reinterpret_cast<const __nv_bfloat162*>(gate + vox * COUT + n);
-        if (!(__low2float(gv) > 0.f)) r0 = 0.f;
-        if (!(__high2float(gv) > 0.f)) r1 = 0.f;
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+      if (s >= 2) {  // groups of stages <= s - 2 complete: at most two pending
+        asm volatile("cp.async.wait_group 2;\n" ::: "memory");
+        land(s - 2);
       }
-      if (epi & EPI_RES) {
-        const __nv_bfloat162 rv = *reinterpret_cast<const __nv_bfloat162*>(res + vox * COUT + n);
-        r0 += __low2float(rv);
-        r1 += __high2float(rv);
-      }
-      store2<OutT>(out + vox * COUT + n, r0, r1);
     }
-  };
-
-  bool failed = false;
-  int issued = 0;  // stages whose MMAs were issued
-  for (int q = 0; q < TC_NBUF - 1; ++q) fetch(q);
-  for (int s = 0; s < nstages; ++s) {
-    const int dy = s % 3, ti = s / 3;
-    // groups committed so far: stages 0 .. s + TC_NBUF - 2; all but the newest TC_NBUF - 2 have landed
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(TC_NBUF - 2) : "memory");
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // cp.async writes -> tensor core reads
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      const uint32_t a_base = smem_u32(sA + (size_t)(s % TC_NBUF) * BUF);
-      const uint32_t d_base = tmem + (uint32_t)((ti & 1) * 64);
-      for (int t = 0; t < 9; ++t) {
-        const int dz = t / 3, dx = t % 3, tap = dy * 9 + t;
-        const uint32_t b0 = smem_u32(sB + (size_t)tap * KC * COUT);
+    if (s == nstages) {  // the last two stages
+      if (nstages >= 2) {
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        land(nstages - 2);
+      }
+      if (nstages >= 1) {
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        land(nstages - 1);
+      }
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  } else if (warp == TC_MMA_WARP) {
+    // ---- MMA issue: one thread
+    if (lane == 0) {
+      const uint32_t idesc = tc_idesc(128, COUT);
+      const uint64_t a_desc0 = tc_smem_desc(smem_u32(sA), A_LBO, A_SBO);
+      const uint64_t b_desc0 = tc_smem_desc(smem_u32(sB), B_LBO, 128);
+      int issued = 0;
+      for (int s = 0; s < nstages; ++s) {
+        const int dy = s % 3, ti = s / 3, acc = ti & 1;
+        // the epilogue of tile ti - 2 has read this accumulator set
+        if (dy == 0 && ti >= 2 && !tc_wait(acc_empty + acc, (uint32_t)((ti / 2 - 1) & 1), abort)) break;
+        if (!tc_wait(full + s % TC_NBUF, (uint32_t)((s / TC_NBUF) & 1), abort)) break;
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint64_t a_desc = a_desc0 + (uint64_t)((s % TC_NBUF) * BUF);  // start address in 16-byte units
+        const uint32_t d_base = tmem + (uint32_t)(acc * 64);
 #pragma unroll
-        for (int ks = 0; ks < CIN / 16; ++ks) {
-          const uint64_t bd = tc_smem_desc(b0 + ks * 2 * B_LBO, B_LBO, 128);
-          const uint32_t acc = (dy > 0 || t > 0 || ks > 0) ? 1u : 0u;
+        for (int t = 0; t < 9; ++t) {
+          const int dz = t / 3, dx = t % 3;
 #pragma unroll
-          for (int h = 0; h < 2; ++h) {  // x-voxels 16h .. 16h+15 of the tile
-            const uint32_t a0 = a_base + (uint32_t)((2 * ks * TC_HALO + (16 * h + dx) * TC_ZR + dz) * 16);
-            const uint64_t ad = tc_smem_desc(a0, A_LBO, A_SBO);
-            asm volatile(
-                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_base + (uint32_t)(h * 32)),
-                "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+          for (int ks = 0; ks < CIN / 16; ++ks) {
+            const uint64_t bd = b_desc0 + (uint64_t)((dy * 9 + t) * KC * COUT + ks * 2 * COUT);
+            const uint32_t accum = (dy > 0 || t > 0 || ks > 0) ? 1u : 0u;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {  // x-voxels 16h .. 16h+15 of the tile
+              const uint64_t ad = a_desc + (uint64_t)(2 * ks * TC_HALO + (16 * h + dx) * TC_ZR + dz);
+              asm volatile(
+                  "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_base + (uint32_t)(h * 32)),
+                  "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+            }
           }
         }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+            smem_u32(empty + s % TC_NBUF)));
+        if (dy == 2)
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+              smem_u32(acc_full + acc)));
+        issued = s + 1;
       }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-          smem_u32(bar + s % TC_NBUF)));
+      // every MMA issued has completed before the accumulators can be freed (the last commit tracks them all)
+      if (issued > 0) {
+        const int q = issued - 1;
+        volatile int no_abort = 0;
+        tc_wait(empty + q % TC_NBUF, (uint32_t)((q / TC_NBUF) & 1), &no_abort);
+        if (no_abort) *abort = 1;
+      }
     }
-    issued = s + 1;
-    if (s >= 1) {
-      // stage s-1's MMAs (the (s-1)/TC_NBUF-th completion of its buffer's mbarrier) have read their halo and,
-      // when s begins a tile, finished the previous tile's accumulators; one decision for the whole CTA
-      const int q = s - 1;
-      const bool ok = tc_wait(bar + q % TC_NBUF, (uint32_t)((q / TC_NBUF) & 1));
-      failed = __syncthreads_or(ok ? 0 : 1) != 0;
-      if (failed) break;
-    }
-    fetch(s + TC_NBUF - 1);  // into buffer (s - 1) % TC_NBUF, free since the wait above
-    if (dy == 0 && ti >= 1) {
+    __syncwarp();
+  } else {
+    // ---- epilogue: warp 4 + g reads TMEM lanes 32 g .. 32 g + 31 of both halves; lane m of half h is the
+    // voxel x = 16 h + m / 8, z = m mod 8 of the tile
+    const int g = warp & 3;
+    for (int ti = 0; ti < my_tiles; ++ti) {
+      const int acc = ti & 1;
+      if (!tc_wait(acc_full + acc, (uint32_t)((ti / 2) & 1), abort)) break;
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      epilogue(ti - 1);  // overlaps stage s's MMAs, which accumulate into the other set
+      const int tile = blockIdx.x + ti * gridDim.x;
+      const int xt = tile % ntx, rest = tile / ntx, zt = rest % ntz, y = rest / ntz;
+      const int m = g * 32 + lane;
+#pragma unroll 1
+      for (int h = 0; h < 2; ++h) {
+        uint32_t r[32];
+        const uint32_t taddr = tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(acc * 64 + h * 32);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+              "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+              "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+              "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        const size_t vox = ((size_t)y * v.Z + zt * TC_TZ + (m & 7)) * v.X + xt * TX + 16 * h + (m >> 3);
+#pragma unroll
+        for (int n = 0; n < COUT; n += 2) {
+          float r0 = __uint_as_float(r[n]), r1 = __uint_as_float(r[n + 1]);
+          if (epi & EPI_BIAS) { r0 += bias[n]; r1 += bias[n + 1]; }
+          if (epi & EPI_RELU) { r0 = fmaxf(r0, 0.f); r1 = fmaxf(r1, 0.f); }
+          if (epi & EPI_GATE) {
+            const __nv_bfloat162 gv = *reinterpret_cast<const __nv_bfloat162*>(gate + vox * COUT + n);
+            if (!(__low2float(gv) > 0.f)) r0 = 0.f;
+            if (!(__high2float(gv) > 0.f)) r1 = 0.f;
+          }
+          if (epi & EPI_RES) {
+            const __nv_bfloat162 rv = *reinterpret_cast<const __nv_bfloat162*>(res + vox * COUT + n);
+            r0 += __low2float(rv);
+            r1 += __high2float(rv);
+          }
+          store2<OutT>(out + vox * COUT + n, r0, r1);
+        }
+      }
       asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+      __syncwarp();
+      if (lane == 0) tc_arrive(acc_empty + acc);
     }
   }
-  if (!failed && nstages > 0) {  // the last tile
-    const int q = nstages - 1;
-    const bool ok = tc_wait(bar + q % TC_NBUF, (uint32_t)((q / TC_NBUF) & 1));
-    failed = __syncthreads_or(ok ? 0 : 1) != 0;
-    if (!failed) {
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      epilogue(my_tiles - 1);
-    }
-  }
-  if (failed && threadIdx.x == 0) atomicExch(err, 1);
-  // MMAs still in flight after a wait ran out: wait (bounded) for the last issued stage, whose commit
-  // follows every earlier MMA, before the accumulators are freed
-  if (failed && issued > 0) tc_wait(bar + (issued - 1) % TC_NBUF, (uint32_t)(((issued - 1) / TC_NBUF) & 1));
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;\n" ::"r"(tmem));
+  if (threadIdx.x == 0 && *abort) atomicExch(err, 1);
+  if (warp == TC_MMA_WARP) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;\n" ::"r"(tmem));
 }
 
 // ---- launchers ---------------------------------------------------------------
@@ -597,7 +644,8 @@ __device__ int g_tc_err;  // set when a tcgen05 convolution's mbarrier wait ran 
 
 template <int CIN, int COUT>
 constexpr size_t tc_smem() {
-  return (size_t)TC_NBUF * (CIN / 8) * TC_HALO * 16 + (size_t)27 * (CIN / 8) * COUT * 16 + TC_NBUF * 8 + 16;
+  // halo ring, weights, 2 TC_NBUF + 4 mbarriers, the TMEM address and the abort flag
+  return (size_t)TC_NBUF * (CIN / 8) * TC_HALO * 16 + (size_t)27 * (CIN / 8) * COUT * 16 + (2 * TC_NBUF + 4) * 8 + 16;
 }
 
 template <int CIN, int COUT, typename OutT>

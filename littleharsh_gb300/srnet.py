@@ -75,7 +75,7 @@ class SRNet:
     """Parameters, activations and the training step on the current CUDA device."""
 
     def __init__(self, params=None, seed: int = 0, nblocks: int = NBLOCKS, lr: float = 1e-3,
-                 betas=(0.9, 0.999), eps: float = 1e-8, weight_decay: float = 0.0, tcgen05: bool = False):
+                 betas=(0.9, 0.999), eps: float = 1e-8, weight_decay: float = 0.0, tcgen05: bool = True):
         torch = _torch()
         self.nblocks = nblocks
         self.shapes = layer_shapes(nblocks)
@@ -106,8 +106,8 @@ class SRNet:
         self.flip = [torch.zeros(27 * vw["ci"] * vw["co"], dtype=torch.bfloat16, device=dev) for vw in self.views]
         self.lr, self.betas, self.eps, self.wd = lr, betas, eps, weight_decay
         self.t = 0
-        # forward and data-gradient convolutions on tcgen05 when set; mma.sync by default, which measures
-        # faster with the present staging of the tcgen05 kernel
+        # forward and data-gradient convolutions on tcgen05 (the default: the warp-specialised TMEM kernel
+        # measures faster than mma.sync in training and inference) or, when unset or Z % 8 != 0, on mma.sync
         self.tcgen05 = tcgen05
         self.sigma = 1.0  # scale of the correction (set by training: rms of the residual it learns)
         self._acts = None

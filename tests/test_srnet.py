@@ -190,7 +190,8 @@ def test_mse_and_adam(lib):
 
 
 @pytest.mark.gpu
-def test_network_gradient_matches_oracle():
+@pytest.mark.parametrize("tcgen05", [True, False], ids=["tcgen05", "mma_sync"])
+def test_network_gradient_matches_oracle(tcgen05):
     import torch
     from littleharsh_gb300 import srnet
     rng = np.random.default_rng(11)
@@ -201,7 +202,7 @@ def test_network_gradient_matches_oracle():
     params[-1][0][:, :3, :] = rng.standard_normal(params[-1][0][:, :3, :].shape) * 0.02
     params = [(so.bf16_round(w * (3.0 if i > 0 else 1.0)), (rng.standard_normal(b.shape) * 0.05).astype(np.float32))
               for i, (w, b) in enumerate(params)]
-    net = srnet.SRNet(params=params)
+    net = srnet.SRNet(params=params, tcgen05=tcgen05)
     x = np.zeros((Y, Z, X, 16), np.float32)
     x[..., :5] = rng.standard_normal((Y, Z, X, 5))
     x = so.bf16_round(x)
@@ -267,13 +268,14 @@ def test_conv_fwd_tcgen05(lib, cin, cout, f32, flags):
 
 
 @pytest.mark.gpu
-def test_conv_fwd_tcgen05_many_tiles_per_cta(lib):
-    """More tiles than SMs: each persistent CTA pipelines several tiles through its two stage buffers."""
+@pytest.mark.parametrize("Y,Z,X", [(80, 16, 64), (96, 32, 128)], ids=["320_tiles", "1536_tiles"])
+def test_conv_fwd_tcgen05_many_tiles_per_cta(lib, Y, Z, X):
+    """More tiles than SMs (tiles of 8 z-rows x 32 x-voxels): each persistent CTA pipelines several tiles
+    through its ring of four halo buffers and its two accumulator sets, which wrap around many times."""
     import ctypes
     import torch
     from littleharsh_gb300 import srnet
     rng = np.random.default_rng(77)
-    Y, Z, X = 80, 16, 64  # 320 tiles of 8 z-rows x 32 x-voxels
     x = so.bf16_round(rng.standard_normal((Y, Z, X, 32)))
     w = so.bf16_round(rng.standard_normal((27, 32, 32)) / np.sqrt(27 * 32))
     b = rng.standard_normal(32).astype(np.float32)
