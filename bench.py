@@ -365,6 +365,7 @@ def run_ours(args, rank: int, world: int, local_rank: int, dist):
                 traffic = json.load(open(tp)).get(f"{args.workload}:{args.precision}:{dom}")
             except Exception:
                 traffic = None
+        c576 = dom == "xprod" and cfg.get("ngalx") == 576 and cfg.get("ngalz") == 576 and "ngalx2" not in cfg
         roof = {"bound": "hbm", "kernel": dom, "achieved": ach_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": (ach_gbs / peaks["hbm_gbs"]) if ach_gbs else None, "traffic": traffic,
                 "peak_src": f"{peaks['src']} (MEASURED_PEAKS.json hbm_gbs)" if peaks["src"] == "measured" else "fallback",
@@ -373,7 +374,13 @@ def run_ours(args, rank: int, world: int, local_rank: int, dist):
             tf = flops_l / (per_launch_ms * 1e-3) / 1e12
             roof["fp64"] = {"achieved": tf, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
                             "frac": tf / peaks["fp64_tflops"], "model_flops_per_launch": flops_l,
-                            "note": "FP64 FMA peak measured on this pool (own probe)"} if prec == lh.PREC_FP64 else \
+                            "note": "FP64 FMA peak measured on this pool (own probe); model flops count an FMA as 2, "
+                                    "while every FP64 addition also takes a full pipe slot",
+                            # ncu of this kernel at configuration 2's transform lengths (a one-resolution
+                            # 576 x 576 grid), where it applies
+                            "pipe_active_ncu": 0.848 if c576 else None,
+                            "pipe_active_src": "ncu sm__pipe_fp64_cycles_active, profiles/k_xprod_xz576_fp64.txt"
+                            if c576 else None} if prec == lh.PREC_FP64 else \
                 {"achieved": tf, "unit": "TFLOP/s (FP32 pipe)", "model_flops_per_launch": flops_l}
         kernels = {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in prof.items()}
         # end to end through the C ABI with host buffers: upload, one step, download
