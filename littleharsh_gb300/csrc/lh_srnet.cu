@@ -373,7 +373,7 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
 // addresses and nothing is copied twice.
 //
 // The CTA is warp-specialised, its roles ordered only by mbarriers:
-//   warps 0-3 (producers) fetch halos with cp.async into a ring of four
+//   warps 0-3 (producers) fetch halos with cp.async into a ring of six
 //     buffers; once a thread's copies for a stage have landed it fences them
 //     for the tensor core and arrives on the buffer's `full` barrier (128
 //     arrivals); a buffer is refilled after the `empty` barrier says the MMAs
@@ -393,7 +393,9 @@ constexpr int TC_TZ = 8;                     // z rows per tile
 constexpr int TC_ZR = TC_TZ + 2;             // halo z rows
 constexpr int TC_XR = TX + 2;                // halo x voxels
 constexpr int TC_HALO = TC_ZR * TC_XR;       // 16-byte rows per k-chunk plane of a halo
-constexpr int TC_NBUF = 4;                   // halo ring
+constexpr int TC_NBUF = 6;                   // halo ring (4: 218 us, 6: 203 us, 8: 201 us on 130x96x96)
+constexpr int TC_LAG = 3;                    // stages between issuing a halo's copies and handing it over
+static_assert(TC_LAG >= 1 && TC_LAG <= 4 && TC_LAG < TC_NBUF, "the producer must be able to run TC_LAG stages ahead");
 constexpr int TC_PRODUCERS = 128;            // warps 0-3
 constexpr int TC_THREADS = 288;              // + epilogue warps 4-7 + MMA warp 8
 constexpr int TC_MMA_WARP = 8;
@@ -510,19 +512,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         cp_async16(buf + ((size_t)kc * TC_XR + xh) * TC_ZR + zz, in + vox * CIN + kc * 8, ok);
       }
       asm volatile("cp.async.commit_group;\n" ::: "memory");
-      if (s >= 2) {  // groups of stages <= s - 2 complete: at most two pending
-        asm volatile("cp.async.wait_group 2;\n" ::: "memory");
-        land(s - 2);
+      if (s >= TC_LAG) {  // groups of stages <= s - TC_LAG complete: at most TC_LAG pending
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(TC_LAG) : "memory");
+        land(s - TC_LAG);
       }
     }
-    if (s == nstages) {  // the last two stages
-      if (nstages >= 2) {
-        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-        land(nstages - 2);
-      }
-      if (nstages >= 1) {
-        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        land(nstages - 1);
+    if (s == nstages) {  // the last TC_LAG stages, oldest first
+      for (int q = nstages - TC_LAG < 0 ? 0 : nstages - TC_LAG; q < nstages; ++q) {
+        const int pending = nstages - 1 - q;
+        if (pending >= 3) asm volatile("cp.async.wait_group 3;\n" ::: "memory");
+        else if (pending == 2) asm volatile("cp.async.wait_group 2;\n" ::: "memory");
+        else if (pending == 1) asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        else asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        land(q);
       }
     }
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");

@@ -271,7 +271,7 @@ def test_conv_fwd_tcgen05(lib, cin, cout, f32, flags):
 @pytest.mark.parametrize("Y,Z,X", [(80, 16, 64), (96, 32, 128)], ids=["320_tiles", "1536_tiles"])
 def test_conv_fwd_tcgen05_many_tiles_per_cta(lib, Y, Z, X):
     """More tiles than SMs (tiles of 8 z-rows x 32 x-voxels): each persistent CTA pipelines several tiles
-    through its ring of four halo buffers and its two accumulator sets, which wrap around many times."""
+    through its ring of six halo buffers and its two accumulator sets, which wrap around many times."""
     import ctypes
     import torch
     from littleharsh_gb300 import srnet
