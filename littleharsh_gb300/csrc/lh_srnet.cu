@@ -603,22 +603,59 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
         const size_t vox = ((size_t)y * v.Z + zt * TC_TZ + (m & 7)) * v.X + xt * TX + 16 * h + (m >> 3);
+        // the voxel's COUT outputs: bias, ReLU, gate, residual in that order; gate, residual and output move
+        // 16 bytes at a time (the entry point requires 16-byte aligned tensors)
+        float o[COUT];
 #pragma unroll
-        for (int n = 0; n < COUT; n += 2) {
-          float r0 = __uint_as_float(r[n]), r1 = __uint_as_float(r[n + 1]);
-          if (epi & EPI_BIAS) { r0 += bias[n]; r1 += bias[n + 1]; }
-          if (epi & EPI_RELU) { r0 = fmaxf(r0, 0.f); r1 = fmaxf(r1, 0.f); }
-          if (epi & EPI_GATE) {
-            const __nv_bfloat162 gv = *reinterpret_cast<const __nv_bfloat162*>(gate + vox * COUT + n);
-            if (!(__low2float(gv) > 0.f)) r0 = 0.f;
-            if (!(__high2float(gv) > 0.f)) r1 = 0.f;
+        for (int n = 0; n < COUT; ++n) {
+          o[n] = __uint_as_float(r[n]);
+          if (epi & EPI_BIAS) o[n] += bias[n];
+          if (epi & EPI_RELU) o[n] = fmaxf(o[n], 0.f);
+        }
+        if (epi & EPI_GATE) {
+          const uint4* gp = reinterpret_cast<const uint4*>(gate + vox * COUT);
+#pragma unroll
+          for (int q = 0; q < COUT / 8; ++q) {
+            const uint4 gv = gp[q];
+            const uint32_t gw[4] = {gv.x, gv.y, gv.z, gv.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const __nv_bfloat162 g2 = *reinterpret_cast<const __nv_bfloat162*>(&gw[e]);
+              if (!(__low2float(g2) > 0.f)) o[8 * q + 2 * e] = 0.f;
+              if (!(__high2float(g2) > 0.f)) o[8 * q + 2 * e + 1] = 0.f;
+            }
           }
-          if (epi & EPI_RES) {
-            const __nv_bfloat162 rv = *reinterpret_cast<const __nv_bfloat162*>(res + vox * COUT + n);
-            r0 += __low2float(rv);
-            r1 += __high2float(rv);
+        }
+        if (epi & EPI_RES) {
+          const uint4* rp = reinterpret_cast<const uint4*>(res + vox * COUT);
+#pragma unroll
+          for (int q = 0; q < COUT / 8; ++q) {
+            const uint4 rv = rp[q];
+            const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const __nv_bfloat162 r2 = *reinterpret_cast<const __nv_bfloat162*>(&rw[e]);
+              o[8 * q + 2 * e] += __low2float(r2);
+              o[8 * q + 2 * e + 1] += __high2float(r2);
+            }
           }
-          store2<OutT>(out + vox * COUT + n, r0, r1);
+        }
+        if constexpr (sizeof(OutT) == 4) {
+          float4* op = reinterpret_cast<float4*>(out + vox * COUT);
+#pragma unroll
+          for (int q = 0; q < COUT / 4; ++q) op[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+        } else {
+          uint4* op = reinterpret_cast<uint4*>(out + vox * COUT);
+#pragma unroll
+          for (int q = 0; q < COUT / 8; ++q) {
+            uint32_t pk[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const __nv_bfloat162 b2 = __floats2bfloat162_rn(o[8 * q + 2 * e], o[8 * q + 2 * e + 1]);
+              pk[e] = *reinterpret_cast<const uint32_t*>(&b2);
+            }
+            op[q] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+          }
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -757,8 +794,8 @@ int lh_sr_conv_fwd_tc(int32_t cin, int32_t cout, const void* in, const void* w, 
     lh::set_init_error("lh_sr_conv_fwd_tc: Z must be a multiple of 8");
     return LH_EINVAL;
   }
-  if (!in || !w || !out || !aligned16(in) || !aligned16(w) || ((flags & 2) && !res) || ((flags & 4) && !gate) ||
-      ((flags & 8) && !bias)) {
+  if (!in || !w || !out || !aligned16(in) || !aligned16(w) || !aligned16(out) || ((flags & 2) && !aligned16(res)) ||
+      ((flags & 4) && !aligned16(gate)) || ((flags & 8) && !bias)) {
     lh::set_init_error("lh_sr_conv_fwd_tc: missing or misaligned pointer");
     return LH_EINVAL;
   }

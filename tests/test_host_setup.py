@@ -123,3 +123,22 @@ def test_header_declares_exported_symbols(lh):
     L = lh.load_library()
     for name in declared:
         assert hasattr(L, name), name
+
+
+def test_tcgen05_convolution_rejects_misaligned_tensors(lh):
+    """The tcgen05 convolution moves its input, output, residual and gate 16 bytes at a time: a tensor that
+    does not start on a 16-byte boundary is refused before anything is launched (addresses only, no GPU)."""
+    L = lh.load_library()
+    ok_in, ok_w, ok_out = 0x10000, 0x20000, 0x30000
+    bias, res, gate = 0x40000, 0x50000, 0x60000
+    BIAS, RES, GATE = 8, 2, 4
+    args = dict(cin=32, cout=32, X=64, Y=4, Z=16)
+
+    def call(inp, w, out, res_p, gate_p, flags):
+        return L.lh_sr_conv_fwd_tc(args["cin"], args["cout"], inp, w, bias, out, 0, res_p, gate_p, flags,
+                                   args["X"], args["Y"], args["Z"], None)
+    assert call(ok_in, ok_w, ok_out + 8, None, None, BIAS) == -1
+    assert call(ok_in + 4, ok_w, ok_out, None, None, BIAS) == -1
+    assert call(ok_in, ok_w, ok_out, res + 2, None, BIAS | RES) == -1
+    assert call(ok_in, ok_w, ok_out, None, gate + 8, BIAS | GATE) == -1
+    assert b"misaligned" in L.lh_last_error(None)
