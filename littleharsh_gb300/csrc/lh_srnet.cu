@@ -365,10 +365,11 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
 // x-voxels, fp32 accumulators of Cout columns in TMEM).  Its work runs as three
 // stages, one per y offset dy of the taps.  A stage's input is the dy level's
 // halo, 34 x-voxels x 10 z-rows, held in shared memory as 16-byte rows
-// [k chunk][x][z] (no-swizzle K-major core matrices of 8 rows x 16 bytes).
-// With z fastest, a core matrix is 8 consecutive z of one x, and consecutive
-// core matrices along M are consecutive x, 10 rows apart; the A operand of tap
-// (dz, dx) is then the same layout started dz + 10 dx rows further on, so the
+// [k chunk][x][z] (no-swizzle K-major core matrices of 8 rows x 16 bytes),
+// x columns 11 rows apart (one row of padding spreads the copies over the
+// banks).  With z fastest, a core matrix is 8 consecutive z of one x, and
+// consecutive core matrices along M are consecutive x, 11 rows apart; the A
+// operand of tap (dz, dx) is the same layout started dz + 11 dx rows on, so the
 // nine taps of a stage read one halo copy through their descriptors' start
 // addresses and nothing is copied twice.
 //
@@ -392,7 +393,9 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
 constexpr int TC_TZ = 8;                     // z rows per tile
 constexpr int TC_ZR = TC_TZ + 2;             // halo z rows
 constexpr int TC_XR = TX + 2;                // halo x voxels
-constexpr int TC_HALO = TC_ZR * TC_XR;       // 16-byte rows per k-chunk plane of a halo
+constexpr int TC_HALO = TC_ZR * TC_XR;       // voxel rows of one k chunk of a halo
+constexpr int TC_XP = TC_ZR + 1;             // x pitch in 16-byte rows: odd, so a warp's copies spread over all banks
+constexpr int TC_KP = TC_XR * TC_XP;         // k-chunk pitch in 16-byte rows
 constexpr int TC_NBUF = 6;                   // halo ring (4: 218 us, 6: 203 us, 8: 201 us on 130x96x96)
 constexpr int TC_LAG = 3;                    // stages between issuing a halo's copies and handing it over
 static_assert(TC_LAG >= 1 && TC_LAG <= 4 && TC_LAG < TC_NBUF, "the producer must be able to run TC_LAG stages ahead");
@@ -437,12 +440,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                   const float* __restrict__ bias, OutT* __restrict__ out, const __nv_bfloat16* __restrict__ res,
                   const __nv_bfloat16* __restrict__ gate, int epi, Vol v, int* __restrict__ err) {
   constexpr int KC = CIN / 8;                       // 16-byte chunks (core-matrix columns) per voxel row
-  constexpr uint32_t A_LBO = TC_HALO * 16;          // next k chunk of a halo
-  constexpr uint32_t A_SBO = TC_ZR * 16;            // next 8 rows along M = next x
+  constexpr uint32_t A_LBO = TC_KP * 16;            // next k chunk of a halo
+  constexpr uint32_t A_SBO = TC_XP * 16;            // next 8 rows along M = next x
   constexpr uint32_t B_LBO = COUT * 16;             // next k chunk of a tap's weights
-  constexpr int BUF = KC * TC_HALO;                 // 16-byte rows per halo buffer
+  constexpr int BUF = KC * TC_KP;                   // 16-byte rows per halo buffer
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint4* sA = reinterpret_cast<uint4*>(smem_raw);   // [TC_NBUF][KC][TC_XR][TC_ZR]
+  uint4* sA = reinterpret_cast<uint4*>(smem_raw);   // [TC_NBUF][KC][TC_XR (pitch TC_XP)][TC_ZR]
   uint4* sB = sA + (size_t)TC_NBUF * BUF;           // [27][KC][COUT]
   uint64_t* full = reinterpret_cast<uint64_t*>(sB + (size_t)27 * KC * COUT);
   uint64_t* empty = full + TC_NBUF;
@@ -509,7 +512,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         gz = gz < 0 ? gz + v.Z : (gz >= v.Z ? gz - v.Z : gz);
         gx = gx < 0 ? gx + v.X : (gx >= v.X ? gx - v.X : gx);
         const size_t vox = ok ? ((size_t)gy * v.Z + gz) * v.X + gx : 0;
-        cp_async16(buf + ((size_t)kc * TC_XR + xh) * TC_ZR + zz, in + vox * CIN + kc * 8, ok);
+        cp_async16(buf + (size_t)kc * TC_KP + xh * TC_XP + zz, in + vox * CIN + kc * 8, ok);
       }
       asm volatile("cp.async.commit_group;\n" ::: "memory");
       if (s >= TC_LAG) {  // groups of stages <= s - TC_LAG complete: at most TC_LAG pending
@@ -553,7 +556,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const uint32_t accum = (dy > 0 || t > 0 || ks > 0) ? 1u : 0u;
 #pragma unroll
             for (int h = 0; h < 2; ++h) {  // x-voxels 16h .. 16h+15 of the tile
-              const uint64_t ad = a_desc + (uint64_t)(2 * ks * TC_HALO + (16 * h + dx) * TC_ZR + dz);
+              const uint64_t ad = a_desc + (uint64_t)(2 * ks * TC_KP + (16 * h + dx) * TC_XP + dz);
               asm volatile(
                   "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
                   "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_base + (uint32_t)(h * 32)),
@@ -684,7 +687,7 @@ __device__ int g_tc_err;  // set when a tcgen05 convolution's mbarrier wait ran 
 template <int CIN, int COUT>
 constexpr size_t tc_smem() {
   // halo ring, weights, 2 TC_NBUF + 4 mbarriers, the TMEM address and the abort flag
-  return (size_t)TC_NBUF * (CIN / 8) * TC_HALO * 16 + (size_t)27 * (CIN / 8) * COUT * 16 + (2 * TC_NBUF + 4) * 8 + 16;
+  return (size_t)TC_NBUF * (CIN / 8) * TC_KP * 16 + (size_t)27 * (CIN / 8) * COUT * 16 + (2 * TC_NBUF + 4) * 8 + 16;
 }
 
 template <int CIN, int COUT, typename OutT>
