@@ -6,7 +6,7 @@ import numpy as np
 
 SMALL = dict(Re=2800.0, alp=1.0, bet=2.0, ngalx=24, ngalz=24, ny=33, dyq=13.6, ppp=5, geometry_type=3,
              posth=0.2, dsty=4, dstx=2, dstz=2, ntilex=4, ntilez=4, flag_ctpress=0)
-# BASELINE configuration 1: 96x96 dealiased, ny=97, 12x6 posts, h=0.2, 2x4 points per post
+# configuration 1: 96x96 dealiased, ny=97, 12x6 posts, h=0.2, 2x4 points per post
 C1 = dict(Re=2800.0, alp=1.0, bet=2.0, ngalx=96, ngalz=96, ny=97, dyq=13.6, ppp=5, geometry_type=3,
           posth=0.2, dsty=16, dstx=2, dstz=4, ntilex=12, ntilez=6, flag_ctpress=0)
 SMOOTH = dict(Re=2800.0, alp=1.0, bet=2.0, ngalx=24, ngalz=24, ny=33, dyq=13.6, ppp=5, geometry_type=0,
