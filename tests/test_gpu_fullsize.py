@@ -1,0 +1,97 @@
+"""Configuration 2 at full size (576 x 576 points, 450 u levels, 48 x 24 posts; ~19 GB per solver), where the
+oracle is too slow to step alongside: properties that do not depend on the size hold after a few RK3 steps.
+
+* the projection leaves the field divergence free (max |div| at round-off);
+* the flow-rate correction holds the flow rate at its target;
+* the field stays real: on the kx = 0 line every kz mode is the conjugate of its -kz partner (to round-off in
+  FP64, to FP32 rounding in the mixed form);
+* the mixed form stays within FP32-level distance of FP64 from the same start;
+* the graph-replayed step equals the same substages launched one by one, bit for bit;
+* the same with the reference's variable-resolution bands (middle band 384 x 384 points).
+"""
+import numpy as np
+import pytest
+
+from tests.helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _start(cfg, precision, seed=1):
+    import littleharsh_gb300 as lh
+    from littleharsh_gb300.initial import initial_field
+    s = lh.Solver(lh.Config(**cfg), precision=precision)
+    g = s.grid
+    s.set_fields(*initial_field(g["yu"], g["yv"], s.nz, s.nkx, s.nyp, seed=seed, kmax=max(s.nkx, s.nz // 2)))
+    s.project()
+    s.set_time(0.0, s.cfl_dt(0.5), 0.0)
+    return s
+
+
+def _hermitian_error(f, lone=()):
+    """max |f(kx=0, -kz) - conj f(kx=0, kz)| over the modes with a partner, relative to max |f|.  The fine
+    set's -N2/2 mode has no partner; with bands neither has the middle band's own -N2/2 mode (its +N2/2 partner
+    is a short column, zero on the middle band's levels), so `lone` leaves that pair out, as the oracle's
+    banded step does."""
+    nz = f.shape[1]
+    kk = np.array([k for k in range(1, nz // 2) if k not in lone])
+    line = f[:, :, 0]
+    return float(np.abs(line[:, nz - kk] - np.conj(line[:, kk])).max() / max(np.abs(f).max(), 1e-300))
+
+
+def _check_properties(s, what, herm_tol=1e-12, lone=()):
+    """herm_tol: FP64 keeps the symmetry to round-off; the mixed form's FP32 transforms compute kz and -kz by
+    different paths, so its symmetry holds to FP32 rounding."""
+    q = s.time()
+    assert s.divmax() < 1e-9, f"{what}: max |div| {s.divmax():.3e}"
+    assert abs(q["Qx"] - q["QxT"]) < 1e-7 * abs(q["QxT"]), f"{what}: flow rate {q['Qx']} vs {q['QxT']}"
+    for name, f in zip(("u1", "u2", "u3", "p"), s.get_fields()):
+        assert np.all(np.isfinite(f)), f"{what} {name}: not finite"
+        e = _hermitian_error(f, lone)
+        assert e < herm_tol, f"{what} {name}: kx = 0 line not Hermitian ({e:.2e})"
+
+
+def test_configuration2_fp64_and_mixed():
+    import littleharsh_gb300 as lh
+    from littleharsh_gb300.workloads import CONFIG2
+    fp = _start(CONFIG2, lh.PREC_FP64)
+    _check_properties(fp, "projected start")
+    mx = lh.Solver(lh.Config(**CONFIG2), precision=lh.PREC_MIXED)
+    mx.set_fields(*fp.get_fields())
+    t = fp.time()
+    mx.set_time(0.0, t["dt"], 0.0, t["QxT"])
+    fp.step(3)
+    mx.step(3)
+    _check_properties(fp, "FP64, 3 steps")
+    _check_properties(mx, "mixed, 3 steps", herm_tol=1e-5)
+    for name, a, b in zip(("u1", "u2", "u3"), mx.get_fields(), fp.get_fields()):
+        assert rel_l2(a, b) < 1e-4, f"mixed vs FP64 {name}: {rel_l2(a, b):.2e}"
+    mx.close()
+    fp.close()
+
+
+def test_configuration2_graph_replay_equals_launch_by_launch():
+    import littleharsh_gb300 as lh
+    from littleharsh_gb300.workloads import CONFIG2
+    a = _start(CONFIG2, lh.PREC_FP64, seed=2)
+    b = lh.Solver(lh.Config(**CONFIG2))
+    b.set_fields(*a.get_fields())
+    t = a.time()
+    b.set_time(0.0, t["dt"], 0.0, t["QxT"])
+    a.step(1)  # captured CUDA graph
+    for k in (1, 2, 3):
+        b.substage(k)  # the same substages, launched one by one
+    for x, y in zip(a.get_fields(), b.get_fields()):
+        np.testing.assert_array_equal(x, y)
+    b.close()
+    a.close()
+
+
+def test_configuration2_with_bands():
+    import littleharsh_gb300 as lh
+    from littleharsh_gb300.workloads import CONFIG2_BANDS
+    s = _start(CONFIG2_BANDS, lh.PREC_FP64, seed=3)
+    s.step(3)
+    n2mid = 2 * CONFIG2_BANDS["ngalz2"] // 3  # the middle band's z modes
+    _check_properties(s, "bands, 3 steps", lone=(n2mid // 2,))
+    s.close()

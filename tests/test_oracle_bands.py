@@ -121,3 +121,24 @@ def test_middle_band_planes_use_their_own_resolution(oracle_mod):
     assert abs(n1[jm, 0, 8]) > 1e-3
     # at the bottom-band level the same field's square has no kx = 8 part
     assert abs(n1[jw, 0, 8]) < 1e-14
+
+
+def test_real_field_except_the_middle_bands_lone_mode(oracle_mod):
+    """The physical field stays real: on the kx = 0 line every kz mode is the conjugate of its -kz partner,
+    except the middle band's own -N2/2 mode, whose +N2/2 partner is a short column (zero on the middle band's
+    levels) -- the same as the lone -N2/2 mode of one resolution."""
+    from littleharsh_gb300.initial import initial_field
+    o = make(oracle_mod, SMALL, **BANDS)
+    g = o.grid()
+    o.set_fields(*initial_field(g["yu"], g["yv"], o.nz, o.nkx, o.nyp, seed=3, kmax=max(o.nkx, o.nz // 2)))
+    o.set_scalars(0.0, 1.0, 0.0)
+    o.project()
+    o.set_scalars(0.0, o.cfl_dt(0.5), 0.0, o.flowrate())
+    o.step(3)
+    nz, lone = o.nz, (2 * BANDS["ngalz2"] // 3) // 2
+    for f in o.get_fields():
+        line = f[:, :, 0]
+        kk = np.array([k for k in range(1, nz // 2) if k != lone])
+        assert np.abs(line[:, nz - kk] - np.conj(line[:, kk])).max() == 0.0
+        # the lone mode's pair is not symmetric on the middle band's levels
+        assert np.abs(line[:, nz - lone] - np.conj(line[:, lone])).max() > 0.0
