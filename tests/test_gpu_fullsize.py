@@ -7,6 +7,7 @@ oracle is too slow to step alongside: properties that do not depend on the size 
   FP64, to FP32 rounding in the mixed form);
 * the mixed form stays within FP32-level distance of FP64 from the same start;
 * the graph-replayed step equals the same substages launched one by one, bit for bit;
+* the plane statistics' mean and mean square equal the (0,0) mode and Parseval's sum of the downloaded spectra;
 * the same with the reference's variable-resolution bands (middle band 384 x 384 points).
 """
 import numpy as np
@@ -67,6 +68,24 @@ def test_configuration2_fp64_and_mixed():
     for name, a, b in zip(("u1", "u2", "u3"), mx.get_fields(), fp.get_fields()):
         assert rel_l2(a, b) < 1e-4, f"mixed vs FP64 {name}: {rel_l2(a, b):.2e}"
     mx.close()
+    # plane statistics at full size against the downloaded spectra: the mean is the (0,0) mode, the mean square
+    # Parseval's sum as the physical field sees it (kx > 0 twice, the kx = 0 line paired with -kz, the lone
+    # -N2/2 mode half), both times the plane's points
+    fp.stats_accumulate()
+    n, st = fp.stats_flush()
+    u1 = fp.get_fields()[0]
+    pts = float(fp.ngx) * float(fp.ngz)
+    nz = u1.shape[1]
+    e = 2.0 * (np.abs(u1[:, :, 1:]) ** 2).sum(axis=(1, 2))
+    line = u1[:, :, 0]
+    kk = np.arange(nz)
+    partner = line[:, (nz - kk) % nz]
+    half = 0.5 * (np.abs(line) ** 2 + (line * partner).real)
+    half[:, nz // 2] = 0.5 * np.abs(line[:, nz // 2]) ** 2
+    e += half.sum(axis=1)
+    assert n == 1
+    np.testing.assert_allclose(st["Um"], pts * u1[:, 0, 0].real, rtol=1e-12, atol=1e-9 * pts)
+    np.testing.assert_allclose(st["U2m"], pts * e, rtol=1e-10, atol=1e-12 * pts)
     fp.close()
 
 
