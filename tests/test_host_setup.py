@@ -142,3 +142,12 @@ def test_tcgen05_convolution_rejects_misaligned_tensors(lh):
     assert call(ok_in, ok_w, ok_out, res + 2, None, BIAS | RES) == -1
     assert call(ok_in, ok_w, ok_out, None, gate + 8, BIAS | GATE) == -1
     assert b"misaligned" in L.lh_last_error(None)
+
+
+def test_geometry_without_forcing_builder_is_refused(lh):
+    """geometry_type 1 and 2 have no forcing builder in the reference's shipped solver: the grid set-up refuses
+    them with LH_EUNSUPPORTED (-2) before any device work."""
+    from tests.helpers import SMALL
+    for gt in (1, 2):
+        with pytest.raises(lh.LhError, match=r"\(-2\)"):
+            lh.Solver(lh.Config(**dict(SMALL, geometry_type=gt)))
