@@ -389,14 +389,18 @@ def run_ours(args, rank: int, world: int, local_rank: int, dist):
         s.get_fields(out=pin)
         tinfo = s.time()
         h2d = sum(a.nbytes for a in pin)
-        e2e_steps = max(1, min(args.steps, 3))
-        rt.cudaDeviceSynchronize()
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
+        e2e_steps = max(1, min(args.steps, 5))
+
+        def e2e_step():
             s.set_fields(*pin)
             s.set_time(tinfo["t"], tinfo["dt"], tinfo["mpgx"], tinfo["QxT"])
             s.step(1)
             s.get_fields(out=pin)
+        e2e_step()  # untimed: first touch of the host path
+        rt.cudaDeviceSynchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
         e2e_sec = (time.perf_counter() - t0) / e2e_steps
         e2e = {"value": world * pts / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
                "ms_per_step": e2e_sec * 1e3}
