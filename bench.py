@@ -505,6 +505,59 @@ def run_srnet(args):
     print(json.dumps(out), flush=True)
 
 
+def run_cufft_compare(args):
+    """The step's transforms against cuFFT (through torch.fft, called only) at the workload's shapes, beside
+    the solver's own per-kernel times of one step: the z-inverse of one substage (u, w on the interior centres,
+    v on the interior faces: nkx columns of ngz-point complex transforms per level and field) and the x
+    transforms of the product pass (3 real inverse and 6 real forward transforms of ngx points per level and
+    z row).  One-resolution workloads only."""
+    import torch
+    import littleharsh_gb300 as lh
+    cfg = WORKLOADS[args.workload]
+    if cfg.get("ngalx2") or cfg.get("ngalz2"):
+        raise SystemExit("--cufft compares one-resolution workloads")
+    out = {"metric": "transform time against cuFFT", "unit": "ms", "workload": args.workload, "cufft": {},
+           "ours_per_launch": {}}
+    for prec, name in ((lh.PREC_FP64, "fp64"), (lh.PREC_MIXED, "fp32")):
+        s, _ = build_solver(cfg, prec, seed=1)
+        prof = s.profile_step()
+        out["ours_per_launch"][name] = {k: prof[k][0] / max(prof[k][1], 1) for k in ("zinv", "xprod")}
+        ngx, ngz, nkx, nlev = s.ngx, s.ngz, s.nkx, s.nyu - 2
+        s.close()
+        cdt, rdt = (torch.complex128, torch.float64) if name == "fp64" else (torch.complex64, torch.float32)
+
+        def timed(fn, reps=5):
+            for _ in range(2):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / reps
+        res = {}
+        A = torch.randn(3 * nlev, ngz, nkx, dtype=cdt, device="cuda")  # z strided by nkx, the solver's layout
+        res["z_inverse_strided"] = timed(lambda: torch.fft.ifft(A, dim=1))
+        Ac = A.permute(0, 2, 1).contiguous()
+        del A
+        res["z_inverse_contiguous"] = timed(lambda: torch.fft.ifft(Ac, dim=2))
+        del Ac
+        torch.cuda.empty_cache()
+        rows = nlev * ngz
+        S = torch.randn(3 * rows, ngx // 2 + 1, dtype=cdt, device="cuda")
+        res["x_c2r_3"] = timed(lambda: torch.fft.irfft(S, n=ngx, dim=1))
+        del S
+        torch.cuda.empty_cache()
+        R = torch.randn(6 * rows, ngx, dtype=rdt, device="cuda")
+        res["x_r2c_6"] = timed(lambda: torch.fft.rfft(R, dim=1))
+        del R
+        torch.cuda.empty_cache()
+        out["cufft"][name] = res
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -517,6 +570,7 @@ def main():
     ap.add_argument("--ensemble", action="store_true", help="configuration 4: 16 replicas in one graph per step")
     ap.add_argument("--srnet", action="store_true", help="the warm start's network kernels (training and inference)")
     ap.add_argument("--sr-small", action="store_true", help="with --srnet: the configuration-1 training step only")
+    ap.add_argument("--cufft", action="store_true", help="the step's transforms against cuFFT at the workload's shapes")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -536,7 +590,9 @@ def main():
             torch.cuda.set_device(0)
         except Exception:
             pass
-    if args.srnet:
+    if args.cufft:
+        run_cufft_compare(args)
+    elif args.srnet:
         run_srnet(args)
     elif args.ensemble:
         run_ensemble(args, rank, world)
