@@ -226,3 +226,22 @@ def test_broadband_field(oracle_mod, cfg):
         assert rel_l2(a, b) < 1e-11, f"fp64 {name}: {rel_l2(a, b):.3e}"
     errs = [rel_l2(a, b) for a, b in zip(sols[1].get_fields(), ref)]
     assert max(errs[:3]) < 2e-6 and errs[3] < 1e-4, f"mixed: {errs}"
+
+
+def test_constant_pressure_gradient(oracle_mod):
+    """flag_ctpress = 1 (input.in's constant-pressure mode): the mean pressure gradient stays at its input
+    value and no flow-rate correction runs; 10 FP64 steps against the oracle."""
+    import littleharsh_gb300 as lh
+    cfg = dict(SMALL, flag_ctpress=1)
+    o = oracle_mod.Oracle(**cfg)
+    u1, u2, u3, p = projected_ic(o, seed=4)
+    dt, mp = o.cfl_dt(0.5), -0.01
+    o.set_fields(u1, u2, u3, p)
+    o.set_scalars(0.0, dt, mp, 0.0)
+    s = lh.Solver(lh.Config(**cfg))
+    s.set_fields(u1, u2, u3, p)
+    s.set_time(0.0, dt, mp, 0.0)
+    o.step(10)
+    s.step(10)
+    _cmp_fields(o, s, 1e-10, "constant pressure gradient, 10 steps")
+    assert s.time()["mpgx"] == mp and o.scalars()["mpgx"] == mp
