@@ -12,9 +12,14 @@ replicas of all ranks).  A "step" is one full RK3 step (three substages).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+With --precision fp64 (the default) the same run also measures the mixed form
+(FP32 transforms, products, nonlinear term and canopy forcing; FP64 solves,
+flow rate and statistics) on the same workload and reports it under "mixed".
+
 --impl reference times the CPU FP64 restatement of the reference's step (the
-Fortran reference cannot be built here) on the host cores, on a bounded
-sample: one RK3 step of the same workload.
+Fortran reference cannot be built here) on all host cores, on a bounded
+sample of the same workload: one untimed step, then the median of up to three
+timed steps.
 """
 from __future__ import annotations
 
@@ -47,6 +52,8 @@ BYTES_PER_POINT_FP64 = 576  # compulsory state traffic per spectral point per RK
 
 
 def _peaks() -> dict:
+    """HBM and bf16 denominators from MEASURED_PEAKS.json (the profiling recipe's fallback if it is absent).
+    The FP64 denominator is measured in the run itself (lh_fp64_peak)."""
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     out = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "src": "fallback"}
     if os.path.exists(p):
@@ -56,9 +63,6 @@ def _peaks() -> dict:
                    "src": "measured"}
         except Exception:
             pass
-    # FP64 FMA peak of this machine's GB300 (own probe: 8 independent FMA chains per
-    # thread, 1216 CTAs x 256 threads, CUDA events): 1.198 TFLOP/s
-    out["fp64_tflops"] = 1.198
     return out
 
 
@@ -222,8 +226,9 @@ def build_solver(cfg: dict, precision: int, seed: int):
     return s, (u1, u2, u3, p)
 
 
-def cpu_baseline(cfg: dict, threads: int) -> dict:
-    """The CPU FP64 restatement on the host cores: one RK3 step of the workload."""
+def cpu_baseline(cfg: dict, threads: int, warmup: int = 1, timed: int = 2) -> dict:
+    """The CPU FP64 restatement on the host cores: `warmup` untimed RK3 steps (first touch of its arrays), then
+    the median of `timed` single-step timings of the same workload."""
     from oracle import pyoracle
     from littleharsh_gb300.initial import initial_field
     pyoracle.build()
@@ -233,38 +238,56 @@ def cpu_baseline(cfg: dict, threads: int) -> dict:
     o.set_scalars(0.0, 1.0, 0.0)
     o.project()
     o.set_scalars(0.0, o.cfl_dt(0.5), 0.0, o.flowrate())
-    t0 = time.perf_counter()
-    o.step(1)
-    sec = time.perf_counter() - t0
+    for _ in range(max(warmup, 0)):
+        o.step(1)
+    secs = []
+    for _ in range(max(timed, 1)):
+        t0 = time.perf_counter()
+        o.step(1)
+        secs.append(time.perf_counter() - t0)
+    sec = statistics.median(secs)
     pts = grid_points(cfg, o.nyu, [x for b in range(5) for x in (o.sz.N[0][b], o.sz.N[1][b], o.sz.N[2][b], o.sz.N[3][b])])
-    return {"value": pts / sec, "unit": UNIT, "cores": threads, "kind": "port", "points": pts,
-            "sample": f"1 RK3 step of {cfg['ngalx']}x{cfg['ngalz']}x{o.nyu} FP64 ({sec:.1f} s)"}
+    return {"value": pts / sec, "unit": UNIT, "cores": threads, "kind": "port", "points": pts, "steps_timed": len(secs),
+            "warmup": max(warmup, 0), "seconds_per_step": secs,
+            "sample": f"median of {len(secs)} single RK3 steps after {max(warmup, 0)} untimed, "
+                      f"{cfg['ngalx']}x{cfg['ngalz']}x{o.nyu} FP64 ({sec:.2f} s per step)"}
 
 
 def run_reference(args, rank: int, world: int):
+    """The reference's CPU path (the C restatement of its step, all host threads) on this arm's workload:
+    a bounded sample, at most 1 warm-up and 3 timed steps."""
     if rank != 0:
         return
     cfg = WORKLOADS[args.workload]
     threads = os.cpu_count() or 1
-    vals = []
-    base = None
-    for _ in range(max(args.warmup, 0)):
-        pass  # the oracle has no warm-up effects worth a full extra step of CPU time
-    for _ in range(max(1, min(args.steps, 2))):
-        base = cpu_baseline(cfg, threads)
-        vals.append(base["value"])
-    v = statistics.median(vals)
-    base["value"] = v
+    base = cpu_baseline(cfg, threads, warmup=min(max(args.warmup, 0), 1), timed=max(1, min(args.steps, 3)))
+    v = base["value"]
     pts = base["points"]
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": len(vals),
-            "warmup": args.warmup, "ms_per_step": 1e3 * pts / v, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded laminar + perturbation field)",
-            "config": {"workload": args.workload, "grid": [cfg["ngalx"], cfg["ngalz"], cfg["ny"] + 2 * cfg["dsty"] + 1],
-                       "note": "CPU FP64 restatement of the reference step (the Fortran/MPI reference does not "
-                               "build here: no Fortran compiler and FOU3D.f90 is missing)"},
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": base["steps_timed"], "warmup": base["warmup"], "ms_per_step": 1e3 * pts / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded laminar + 10% perturbation, projected divergence-free)",
+            "config": _config(args, cfg, world),
+            "note": "CPU FP64 restatement of the reference step (the Fortran/MPI reference does not build here: no "
+                    "Fortran compiler and FOU3D.f90 is missing)",
             "cpu_baseline": base,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def _config(args, cfg: dict, world: int) -> dict:
+    """The workload description both arms print (identical keys and values)."""
+    nyu = cfg["ny"] + 2 * cfg["dsty"] + 1
+    nkx, nz = cfg["ngalx"] // 3 + 1, 2 * (cfg["ngalz"] // 3)
+    return {"workload": args.workload, "grid_phys": [cfg["ngalx"], cfg["ngalz"], nyu],
+            "modes": [2 * (cfg["ngalx"] // 3), nz], "posts": [cfg["ntilex"], cfg["ntilez"]],
+            "post_height": cfg["posth"], "Re_b": cfg["Re"], "precision": args.precision,
+            "parallelism": f"replicas x{world}",
+            "l2": (f"inputs larger than L2 ({16 * nkx * nz * nyu / 1e6:.0f} MB per field)"
+                   if 16 * nkx * nz * nyu > 129e6 else
+                   f"fields of {16 * nkx * nz * nyu / 1e6:.0f} MB fit in L2 (a small case: no L2 flush between steps)"),
+            "bands": [cfg.get("ngalx2") or cfg["ngalx"], cfg.get("ngalz2") or cfg["ngalz"]]
+            if cfg.get("ngalx2") else None}
 
 
 def run_ensemble(args, rank: int, world: int):
@@ -302,128 +325,197 @@ def run_ensemble(args, rank: int, world: int):
         m.close()
 
 
-def run_ours(args, rank: int, world: int, local_rank: int, dist):
-    import littleharsh_gb300 as lh
-    cfg = WORKLOADS[args.workload]
-    prec = lh.PREC_MIXED if args.precision == "mixed" else lh.PREC_FP64
-    s, ic = build_solver(cfg, prec, seed=1 + rank)
-    pts = grid_points(cfg, s.nyu, list(s.params.N))
-    if args.warmup > 0:
-        s.step(args.warmup)
+def _model_per_launch(cfg: dict, s, prof: dict, csz: int) -> dict:
+    """Compulsory bytes and model FLOPs per launch of each pipeline kernel, summed over the bands' planes (one
+    band without variable resolution) and divided by the kernel's launches per step.  csz = bytes of one complex
+    value of the mixed planes (16 FP64, 8 mixed)."""
+    npl = s.nkx * s.nz
+    model_step = {"zinv": [0, 0.0], "xprod": [0, 0.0], "zfwd": [0, 0.0]}
+    for (gx, gz, kx, kz, nc, nf) in band_geometry(cfg, s):
+        mpb = kx * gz
+        prune = gz % 3 == 0 and kz * 3 == 2 * gz
+        model_step["zinv"][0] += 3 * (2 * nc + nf) * (kx * kz * 16 + mpb * csz)
+        model_step["zinv"][1] += 3 * z_flops(gz, kx, 2 * nc + nf)
+        model_step["xprod"][0] += 3 * (2 * nc + nf + 4 * nc + 2 * nf) * mpb * csz
+        model_step["xprod"][1] += 3 * xprod_flops(gx, gz, kx, nc)
+        model_step["zfwd"][0] += 3 * (4 * nc + 2 * nf) * (mpb * csz + kx * kz * 16)
+        model_step["zfwd"][1] += 3 * z_flops(gz, kx, 4 * nc + 2 * nf, prune_last=prune)
+    model_step["assemble"] = [3 * 19 * s.nyu * npl * 16, 0.0]
+    model_step["vsolve"] = [3 * 4 * (2 * s.nyu + s.nyv) * npl * 16, 0.0]
+    model_step["psolve"] = [3 * ((16 + 16 + 16 + 8 + 8) * s.nyp * npl + 14 * 16 * s.nyp * npl), 0.0]
+    return {k: (v[0] / max(prof.get(k, (0.0, 1))[1], 1), v[1] / max(prof.get(k, (0.0, 1))[1], 1))
+            for k, v in model_step.items()}
+
+
+def _traffic(workload: str, precision: str, kernel: str):
+    """DRAM bytes per launch of `kernel` from one ncu capture (profiles/traffic.json), or None."""
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(tp):
+        return None, None
+    try:
+        d = json.load(open(tp))
+    except Exception:
+        return None, None
+    key = f"{workload}:{precision}:{kernel}"
+    v = d.get(key)
+    src = d.get("source", {})
+    return v, (src.get(key) if v is not None and isinstance(src, dict) else None)
+
+
+def _timed_steps(s, steps: int, warmup: int, dist, rt, clock_index: int):
+    """W untimed steps, then K steps in one call bracketed by a barrier and device synchronisation on both sides;
+    the solver's own CUDA events (on its stream) time the K graph launches.  Returns (ms, launches per step,
+    clocks sampled during the timed region)."""
+    if warmup > 0:
+        s.step(warmup)
 
     def barrier():
         if dist is not None:
             dist.barrier()
-
-    import ctypes
-    rt = ctypes.CDLL("libcudart.so")
     rt.cudaDeviceSynchronize()
-    sampler = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local_rank)).split(",")[0])
-                           if world == 1 else local_rank)
+    sampler = ClockSampler(clock_index)
     barrier()
     rt.cudaDeviceSynchronize()
     sampler.start()
-    s.step(args.steps)  # K graph launches bracketed by CUDA events on the solver's stream
+    s.step(steps)
     rt.cudaDeviceSynchronize()
     barrier()
     clocks = sampler.stop()
     ms, launches = s.last_step_ms()
-    ms_max = max_over_ranks(ms, dist, f"cuda:{local_rank}")
-    value = whole_job_value(world, pts, args.steps, ms_max)
-    out = None
-    if rank == 0:
-        peaks = _peaks()
-        prof = s.profile_step()
-        dom = max(prof, key=lambda k: prof[k][0])
-        dms, dn = prof[dom]
-        per_launch_ms = dms / max(dn, 1)
-        csz = 16 if prec == lh.PREC_FP64 else 8
-        npl = s.nkx * s.nz
-        # compulsory bytes and model FLOPs per step of each pipeline kernel, summed over the bands' planes
-        # (one band without variable resolution), then divided by the kernel's launches per step
-        model_step = {"zinv": [0, 0.0], "xprod": [0, 0.0], "zfwd": [0, 0.0]}
-        for (gx, gz, kx, kz, nc, nf) in band_geometry(cfg, s):
-            mpb = kx * gz
-            prune = gz % 3 == 0 and kz * 3 == 2 * gz
-            model_step["zinv"][0] += 3 * (2 * nc + nf) * (kx * kz * 16 + mpb * csz)
-            model_step["zinv"][1] += 3 * z_flops(gz, kx, 2 * nc + nf)
-            model_step["xprod"][0] += 3 * (2 * nc + nf + 4 * nc + 2 * nf) * mpb * csz
-            model_step["xprod"][1] += 3 * xprod_flops(gx, gz, kx, nc)
-            model_step["zfwd"][0] += 3 * (4 * nc + 2 * nf) * (mpb * csz + kx * kz * 16)
-            model_step["zfwd"][1] += 3 * z_flops(gz, kx, 4 * nc + 2 * nf, prune_last=prune)
-        model_step["assemble"] = [3 * 19 * s.nyu * npl * 16, 0.0]
-        model_step["vsolve"] = [3 * 4 * (2 * s.nyu + s.nyv) * npl * 16, 0.0]
-        model_step["psolve"] = [3 * ((16 + 16 + 16 + 8 + 8) * s.nyp * npl + 14 * 16 * s.nyp * npl), 0.0]
-        model = {k: (v[0] / max(prof.get(k, (0.0, 1))[1], 1), v[1] / max(prof.get(k, (0.0, 1))[1], 1))
-                 for k, v in model_step.items()}
-        bytes_l, flops_l = model.get(dom, (0, 0.0))
-        ach_gbs = bytes_l / (per_launch_ms * 1e-3) / 1e9 if bytes_l else None
-        traffic = None
-        tp = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(tp):
-            try:
-                traffic = json.load(open(tp)).get(f"{args.workload}:{args.precision}:{dom}")
-            except Exception:
-                traffic = None
-        c576 = dom == "xprod" and cfg.get("ngalx") == 576 and cfg.get("ngalz") == 576 and "ngalx2" not in cfg
-        roof = {"bound": "hbm", "kernel": dom, "achieved": ach_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": (ach_gbs / peaks["hbm_gbs"]) if ach_gbs else None, "traffic": traffic,
-                "peak_src": f"{peaks['src']} (MEASURED_PEAKS.json hbm_gbs)" if peaks["src"] == "measured" else "fallback",
-                "per_launch_ms": per_launch_ms, "algorithmic_bytes_per_launch": bytes_l}
-        if flops_l:
-            tf = flops_l / (per_launch_ms * 1e-3) / 1e12
-            roof["fp64"] = {"achieved": tf, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
-                            "frac": tf / peaks["fp64_tflops"], "model_flops_per_launch": flops_l,
-                            "note": "FP64 FMA peak measured on this pool (own probe); model flops count an FMA as 2, "
-                                    "while every FP64 addition also takes a full pipe slot",
-                            # ncu of this kernel at configuration 2's transform lengths (a one-resolution
-                            # 576 x 576 grid), where it applies
-                            "pipe_active_ncu": 0.848 if c576 else None,
-                            "pipe_active_src": "ncu sm__pipe_fp64_cycles_active, profiles/k_xprod_xz576_fp64.txt"
-                            if c576 else None} if prec == lh.PREC_FP64 else \
-                {"achieved": tf, "unit": "TFLOP/s (FP32 pipe)", "model_flops_per_launch": flops_l}
-        kernels = {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in prof.items()}
-        # end to end through the C ABI with host buffers: upload, one step, download
-        import torch
-        pin = [torch.empty(a.shape, dtype=torch.complex128, pin_memory=True).numpy() for a in ic]
-        s.get_fields(out=pin)
-        tinfo = s.time()
-        h2d = sum(a.nbytes for a in pin)
-        e2e_steps = max(1, min(args.steps, 5))
+    return ms, launches, clocks
 
-        def e2e_step():
-            s.set_fields(*pin)
-            s.set_time(tinfo["t"], tinfo["dt"], tinfo["mpgx"], tinfo["QxT"])
-            s.step(1)
-            s.get_fields(out=pin)
-        e2e_step()  # untimed: first touch of the host path
-        rt.cudaDeviceSynchronize()
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            e2e_step()
-        e2e_sec = (time.perf_counter() - t0) / e2e_steps
-        e2e = {"value": world * pts / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": h2d,
-               "ms_per_step": e2e_sec * 1e3}
-        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-               "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-               "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == lh.PREC_FP64 else "mixed f32/f64",
-               "data": "synthetic (seeded laminar + 10% perturbation, projected divergence-free)",
-               "config": {"workload": args.workload, "grid_phys": [s.ngx, s.ngz, s.nyu],
-                          "modes": [2 * (s.nkx - 1), s.nz], "spectral_points": s.nkx * s.nz * s.nyu,
-                          "parallelism": f"replicas x{world}",
-                          "l2": f"inputs larger than L2 ({16 * s.nkx * s.nz * s.nyu / 1e6:.0f} MB per field)",
-                          "precision": args.precision, "launch_shapes": getattr(s, "tuned", None),
-                          "bands": [cfg.get("ngalx2") or cfg["ngalx"], cfg.get("ngalz2") or cfg["ngalz"]]
-                          if cfg.get("ngalx2") else None},
-               "gpu_launches": launches * args.steps, "e2e": e2e, "roofline": roof, "kernels_ms_per_step": kernels,
-               "clocks": clocks}
-        if not args.no_cpu_baseline and world == 1:
-            try:
-                out["cpu_baseline"] = cpu_baseline(cfg, os.cpu_count() or 1)
-            except Exception as e:  # reported, never fatal to the GPU number
-                out["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
-        print(json.dumps(out), flush=True)
+
+def _e2e(s, ic, steps: int, world: int, pts: int) -> dict:
+    """The metric end to end through the C ABI with host buffers: every step uploads u, v, w, p from pinned host
+    memory (lh_set_fields), advances one RK3 step and downloads the four fields (lh_get_fields); one untimed
+    pass, then up to 5 timed steps."""
+    import torch
+    pin = [torch.empty(a.shape, dtype=torch.complex128, pin_memory=True).numpy() for a in ic]
+    s.get_fields(out=pin)
+    tinfo = s.time()
+    nbytes = sum(a.nbytes for a in pin)
+    n = max(1, min(steps, 5))
+
+    def one():
+        s.set_fields(*pin)
+        s.set_time(tinfo["t"], tinfo["dt"], tinfo["mpgx"], tinfo["QxT"])
+        s.step(1)
+        s.get_fields(out=pin)
+    one()
+    t0 = time.perf_counter()
+    for _ in range(n):
+        one()
+    sec = (time.perf_counter() - t0) / n
+    return {"value": world * pts / sec, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+            "ms_per_step": sec * 1e3, "steps_timed": n}
+
+
+def _roofline(args, cfg, s, prec_name: str, prof: dict, peaks: dict, fp64_peak: float | None) -> dict:
+    """The dominant kernel's rooflines: algorithmic HBM bytes and model FLOPs per launch over its average launch
+    time (per-kernel CUDA events of one step launched kernel by kernel).  The FP64 kernels are bound by the FP64
+    pipe on this part (about one FP64 instruction per 8 bytes of HBM traffic), so the line reports that roofline
+    when its fraction is the larger, with the HBM one beside it."""
+    dom = max(prof, key=lambda k: prof[k][0])
+    dms, dn = prof[dom]
+    per_launch_ms = dms / max(dn, 1)
+    model = _model_per_launch(cfg, s, prof, 16 if prec_name == "fp64" else 8)
+    bytes_l, flops_l = model.get(dom, (0, 0.0))
+    ach_gbs = bytes_l / (per_launch_ms * 1e-3) / 1e9 if bytes_l else None
+    traffic, tsrc = _traffic(args.workload, prec_name, dom)
+    hbm = {"achieved": ach_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+           "frac": (ach_gbs / peaks["hbm_gbs"]) if ach_gbs else None,
+           "peak_src": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks["src"] == "measured" else "fallback 6.8 TB/s"}
+    roof = {"kernel": dom, "per_launch_ms": per_launch_ms, "algorithmic_bytes_per_launch": bytes_l,
+            "traffic": traffic, "traffic_src": tsrc}
+    fp64 = None
+    if flops_l and prec_name == "fp64" and fp64_peak:
+        tf = flops_l / (per_launch_ms * 1e-3) / 1e12
+        fp64 = {"achieved": tf, "peak": fp64_peak, "unit": "TFLOP/s", "frac": tf / fp64_peak,
+                "model_flops_per_launch": flops_l,
+                "peak_src": "measured in this run by the library's FP64 FMA probe (lh_fp64_peak)",
+                "note": "model flops count an FMA as 2; every FP64 addition of the butterflies also takes a full "
+                        "pipe slot, so the pipe is busier than this fraction"}
+        c576 = dom == "xprod" and cfg.get("ngalx") == 576 and cfg.get("ngalz") == 576 and not cfg.get("ngalx2")
+        if c576:
+            fp64["pipe_active_ncu"] = 0.848
+            fp64["pipe_active_src"] = ("profiles/k_xprod_xz576_fp64.txt: ncu sm__pipe_fp64_cycles_active of this "
+                                       "kernel at configuration 2's transform lengths (a committed capture, not "
+                                       "measured in this run)")
+    if fp64 is not None and hbm["frac"] is not None and fp64["frac"] > hbm["frac"]:
+        roof.update({"bound": "fp64", "achieved": fp64["achieved"], "peak": fp64["peak"], "unit": "TFLOP/s",
+                     "frac": fp64["frac"], "fp64": fp64, "hbm": hbm})
+    else:
+        roof.update({"bound": "hbm", "achieved": hbm["achieved"], "peak": hbm["peak"], "unit": "GB/s",
+                     "frac": hbm["frac"], "hbm": hbm})
+        if fp64 is not None:
+            roof["fp64"] = fp64
+        elif flops_l:
+            roof["fp32_model_tflops"] = flops_l / (per_launch_ms * 1e-3) / 1e12
+    return roof
+
+
+def _measure(args, cfg, prec: int, prec_name: str, rank: int, world: int, local_rank: int, dist, rt, peaks,
+             fp64_peak):
+    """One precision on the workload: device-timed K steps (max over ranks), then on rank 0 the per-kernel
+    profile, the roofline and the end-to-end metric."""
+    s, ic = build_solver(cfg, prec, seed=1 + rank)
+    pts = grid_points(cfg, s.nyu, list(s.params.N))
+    clock_index = (int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local_rank)).split(",")[0])
+                   if world == 1 else local_rank)
+    ms, launches, clocks = _timed_steps(s, args.steps, args.warmup, dist, rt, clock_index)
+    ms_max = max_over_ranks(ms, dist, f"cuda:{local_rank}")
+    res = {"value": whole_job_value(world, pts, args.steps, ms_max), "ms_per_step": ms_max / args.steps,
+           "gpu_launches": launches * args.steps, "clocks": clocks, "launch_shapes": getattr(s, "tuned", None),
+           "grid": [s.ngx, s.ngz, s.nyu], "modes": [2 * (s.nkx - 1), s.nz], "spectral_points": s.nkx * s.nz * s.nyu}
+    if rank == 0:
+        prof = s.profile_step()
+        res["roofline"] = _roofline(args, cfg, s, prec_name, prof, peaks, fp64_peak)
+        res["kernels_ms_per_step"] = {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in prof.items()}
+        res["e2e"] = _e2e(s, ic, args.steps, world, pts)
     s.close()
+    return res
+
+
+def run_ours(args, rank: int, world: int, local_rank: int, dist):
+    import ctypes
+
+    import littleharsh_gb300 as lh
+    cfg = WORKLOADS[args.workload]
+    rt = ctypes.CDLL("libcudart.so")
+    peaks = _peaks()
+    fp64_peak = lh.fp64_peak() if rank == 0 else None
+    main_prec = args.precision
+    prec = lh.PREC_MIXED if main_prec == "mixed" else lh.PREC_FP64
+    r = _measure(args, cfg, prec, main_prec, rank, world, local_rank, dist, rt, peaks, fp64_peak)
+    mixed = None
+    if main_prec == "fp64" and not args.no_mixed:
+        # the mixed form (FP32 transforms, products, nonlinear term and canopy forcing; FP64 solves, flow rate,
+        # statistics) on the same workload, same protocol
+        mixed = _measure(args, cfg, lh.PREC_MIXED, "mixed", rank, world, local_rank, dist, rt, peaks, fp64_peak)
+    if rank != 0:
+        return
+    out = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64" if main_prec == "fp64" else "mixed f32/f64",
+           "data": "synthetic (seeded laminar + 10% perturbation, projected divergence-free)",
+           "config": _config(args, cfg, world), "launch_shapes": r["launch_shapes"],
+           "gpu_launches": r["gpu_launches"], "e2e": r["e2e"], "roofline": r["roofline"],
+           "kernels_ms_per_step": r["kernels_ms_per_step"], "clocks": r["clocks"],
+           "fp64_peak_tflops": fp64_peak}
+    if mixed is not None:
+        out["mixed"] = {"value": mixed["value"], "unit": UNIT, "ms_per_step": mixed["ms_per_step"],
+                        "speedup_vs_fp64": r["ms_per_step"] / mixed["ms_per_step"], "dtype": "mixed f32/f64",
+                        "e2e": mixed["e2e"], "gpu_launches": mixed["gpu_launches"], "clocks": mixed["clocks"],
+                        "roofline": mixed["roofline"], "kernels_ms_per_step": mixed["kernels_ms_per_step"],
+                        "launch_shapes": mixed["launch_shapes"],
+                        "precision": "FP32 transforms, products, nonlinear term and canopy forcing; FP64 viscous "
+                                     "and pressure terms, Helmholtz and pressure solves, flow rate, statistics"}
+    if not args.no_cpu_baseline and world == 1:
+        try:
+            out["cpu_baseline"] = cpu_baseline(cfg, os.cpu_count() or 1)
+        except Exception as e:  # reported, never fatal to the GPU number
+            out["cpu_baseline"] = {"value": None, "error": str(e)[:200]}
+    print(json.dumps(out), flush=True)
 
 
 def srnet_flops(Y: int, Z: int, X: int, train: bool) -> float:
@@ -567,6 +659,7 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="with --precision fp64: skip the mixed form's line")
     ap.add_argument("--ensemble", action="store_true", help="configuration 4: 16 replicas in one graph per step")
     ap.add_argument("--srnet", action="store_true", help="the warm start's network kernels (training and inference)")
     ap.add_argument("--sr-small", action="store_true", help="with --srnet: the configuration-1 training step only")

@@ -126,8 +126,34 @@ int lh_get_time(lh_handle* h, double* out5);
 
 /* Advance nsteps full RK3 steps (the body of the main loop,
  * littleharsh.f90:164-199) with the current dt.  The device work of one step
- * is captured once into a CUDA graph and replayed. */
+ * is captured once into a CUDA graph and replayed.  Returns LH_ENUMERIC when
+ * a NaN or an infinity reached the fields (the pressure solve, which sees the
+ * divergence of every column, flags it on the device at no extra pass; the
+ * flag is read once per call, or once per monitor block), or when the
+ * monitor's max |div| exceeds maxerr; lh_last_error names the steps.  The
+ * fields are left as they are for inspection; uploading fields clears the
+ * flag. */
 int lh_rk3_step(lh_handle* h, int32_t nsteps);
+
+/* Step monitor.  The reference computes max |div| after each substage's
+ * correction (v_corr, littleharsh.f90:933-935) and reports it through
+ * `error` (littleharsh.f90:323-352) against input.in's maxerr
+ * (start.f90:160,430).  With every > 0, lh_rk3_step runs its steps in blocks
+ * of `every`, and after each block computes max |div| on the device and
+ * returns LH_ENUMERIC if it exceeds maxerr; every = 0 (the default) turns the
+ * monitor off.  The monitor's kernels run outside the timed graph launches
+ * (lh_last_step_ms excludes them). */
+int lh_set_monitor(lh_handle* h, double maxerr, int32_t every);
+/* The last max |div| the monitor measured (-1 before its first block) and the
+ * device's sticky error bits (1 = non-finite value).  Either pointer may be
+ * NULL.  No counterpart in the reference beyond `error`'s err. */
+int lh_get_monitor(lh_handle* h, double* divmax, int32_t* err_bits);
+
+/* FP64 FMA throughput of the current device in TFLOP/s, measured by a probe
+ * kernel of this library (eight independent FMA chains per thread, best of
+ * three CUDA-event-timed launches); the denominator of the FP64 roofline the
+ * benchmark reports.  No counterpart in the reference. */
+int lh_fp64_peak(double* tflops);
 
 /* One substage kRK (1..3) up to `upto` (1 right-hand sides divided by axz,
  * 2 after the canopy forcing, 3 after the velocity solves, 4 after the
@@ -223,11 +249,16 @@ int lh_get_launch_shapes(lh_handle* h, int32_t* tx, int32_t* chunk, int32_t* xsp
  * limits the grid to about 48 bytes x nyp x (N1/2+1) x N2 <= 64 MiB
  * (configuration 1 fits, configuration 2 does not); larger grids return
  * LH_EINVAL with the reason in lh_last_error(NULL).  prm, yu, dthdyu and
- * dthdyv are the host arrays lh_init takes; dt only scales psi (it cancels).
- * The first call on a device looks up the array's device address, so make it
- * before any stream capture.  All calls share the array: calls whose work
- * overlaps on the GPU race.  Runs on `stream` (cudaStream_t, NULL = default)
- * of the current device and returns after the projection has finished. */
+ * dthdyv are the host arrays lh_init takes, checked as lh_init checks them;
+ * grids with two x/z resolutions return LH_EUNSUPPORTED.  dt only scales psi
+ * (it cancels).  Every call looks up the array's device address on the
+ * current device.  With lazy module loading (CUDA_MODULE_LOADING=LAZY, the
+ * default) the 64 MiB is placed on a device at the first call there, not when
+ * the library loads.  The call copies tables from host memory and waits for
+ * its stream, so it cannot be made while that stream is capturing a graph.
+ * All calls share the array: calls whose work overlaps on the GPU race.  Runs
+ * on `stream` (cudaStream_t, NULL = default) of the current device and
+ * returns after the projection has finished. */
 int lh_project_noalloc(const lh_params* prm, const double* yu, const double* dthdyu, const double* dthdyv,
                        double* u1, double* u2, double* u3, double dt, void* stream);
 

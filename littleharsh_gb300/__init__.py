@@ -31,7 +31,7 @@ EXPORTED_SYMBOLS = [
     "lh_get_nonlinear", "lh_set_time", "lh_get_time", "lh_rk3_step", "lh_substage", "lh_get_rhs", "lh_divmax",
     "lh_cfl_dt", "lh_project", "lh_spectra_accumulate", "lh_spectra_flush", "lh_stats_accumulate",
     "lh_stats_flush", "lh_cond_accumulate", "lh_cond_flush", "lh_last_step_ms", "lh_profile_step",
-    "lh_project_noalloc", "lh_ensemble_create", "lh_ensemble_step", "lh_ensemble_last_error",
+    "lh_project_noalloc", "lh_set_monitor", "lh_get_monitor", "lh_fp64_peak", "lh_ensemble_create", "lh_ensemble_step", "lh_ensemble_last_error",
     "lh_ensemble_free", "lh_autotune", "lh_get_launch_shapes", "lh_write_restart", "lh_read_restart", "lh_write_stats", "lh_write_spectra", "lh_read_input", "lh_setup_grid", "lh_setup_canopy",
     # include/lh_srnet.h: kernels of the learned warm start
     "lh_sr_conv_fwd", "lh_sr_conv_fwd_tc", "lh_sr_tc_status", "lh_sr_conv_wgrad", "lh_sr_flip_weights", "lh_sr_mse", "lh_sr_adam",
@@ -39,7 +39,14 @@ EXPORTED_SYMBOLS = [
 
 
 class LhError(RuntimeError):
-    pass
+    """A failed call; `code` is the LH_E* return code (None when not from a call)."""
+
+    def __init__(self, msg: str, code: int | None = None):
+        super().__init__(msg)
+        self.code = code
+
+
+LH_EINVAL, LH_EUNSUPPORTED, LH_EFFT, LH_ECUDA, LH_ENOMEM, LH_ESTATE, LH_ENUMERIC = -1, -2, -3, -4, -5, -6, -7
 
 
 class Params(C.Structure):
@@ -104,6 +111,9 @@ def load_library(build: bool = True) -> C.CDLL:
     L.lh_set_time.argtypes = [vp] + [C.c_double] * 4
     L.lh_get_time.argtypes = [vp, _dp]
     L.lh_rk3_step.argtypes = [vp, i32]
+    L.lh_set_monitor.argtypes = [vp, C.c_double, i32]
+    L.lh_get_monitor.argtypes = [vp, _dp, C.POINTER(i32)]
+    L.lh_fp64_peak.argtypes = [_dp]
     L.lh_substage.argtypes = [vp, i32, i32]
     L.lh_divmax.argtypes = [vp, _dp]
     L.lh_cfl_dt.argtypes = [vp, C.c_double, _dp]
@@ -248,7 +258,7 @@ class Solver:
 
     def _check(self, rc):
         if rc:
-            raise LhError(f"littleharsh call failed ({rc}): {load_library().lh_last_error(self.h).decode()}")
+            raise LhError(f"littleharsh call failed ({rc}): {load_library().lh_last_error(self.h).decode()}", rc)
 
     def close(self):
         if getattr(self, "h", None):
@@ -312,6 +322,17 @@ class Solver:
 
     def step(self, n: int = 1):
         self._check(load_library().lh_rk3_step(self.h, n))
+
+    def set_monitor(self, maxerr: float, every: int = 1):
+        """Check max |div| against maxerr every `every` steps (0 = off); a step that exceeds it, or that
+        leaves a NaN or infinity in the fields, raises LhError with code LH_ENUMERIC."""
+        self._check(load_library().lh_set_monitor(self.h, maxerr, every))
+
+    def monitor(self) -> dict:
+        """The monitor's last max |div| (-1 before its first check) and the device's error bits."""
+        d, e = C.c_double(0), C.c_int32(0)
+        self._check(load_library().lh_get_monitor(self.h, C.byref(d), C.byref(e)))
+        return {"divmax": d.value, "err_bits": e.value}
 
     def substage(self, krk: int, upto: int = 5):
         self._check(load_library().lh_substage(self.h, krk, upto))
@@ -459,6 +480,16 @@ class Ensemble:
             self.close()
         except Exception:
             pass
+
+
+def fp64_peak() -> float:
+    """FP64 FMA throughput of the current device in TFLOP/s, measured by the library's probe kernel."""
+    L = load_library()
+    o = C.c_double(0)
+    rc = L.lh_fp64_peak(C.byref(o))
+    if rc:
+        raise LhError(f"lh_fp64_peak failed ({rc}): {L.lh_last_error(None).decode()}", rc)
+    return o.value
 
 
 from .initial import initial_field  # noqa: E402

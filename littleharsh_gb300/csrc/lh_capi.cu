@@ -89,6 +89,10 @@ struct lh_handle {
   unsigned long long graph_gen = 0;  // bumped whenever captured launch arguments (dt) change
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0;
+  // step monitor (lh_set_monitor): max |div| checked against maxerr every mon_every steps (0 = off)
+  double mon_maxerr = 0;
+  int mon_every = 0;
+  double last_divmax = -1;
   int launches_per_step = 0;
   // per-launch timing (lh_profile_step): kind of each launch and the event recorded after it
   bool profiling = false;
@@ -481,7 +485,7 @@ int enqueue_substage(lh_handle* h, int k, int upto) {
   const double dti = 1.0 / h->dt;
   const double dtirk = dti / (h->aRK[k] + h->bRK[k]);
   const double dtrk = h->dt * (h->aRK[k] + h->bRK[k]);
-  launch_psolve(h->u1, h->u2, h->u3, h->p, h->psi, d, h->t, dtirk, dtrk, h->gw[0][0], h->gw[2][1], st);
+  launch_psolve(h->u1, h->u2, h->u3, h->p, h->psi, d, h->t, dtirk, dtrk, h->gw[0][0], h->gw[2][1], h->sc, st);
   mark(h, K_PSOLVE);
   return LH_OK;
 }
@@ -561,9 +565,76 @@ int host_flowrate(lh_handle* h, double* Q) {
   return LH_OK;
 }
 
+// The sticky error bits of the device scalars (read after the stream has finished).
+int read_err(lh_handle* h, int* err) {
+  CU(h, cudaMemcpyAsync(err, &h->sc->err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CU(h, cudaStreamSynchronize(h->st));
+  return LH_OK;
+}
+
+// error (littleharsh.f90:323-352): max |div u| over the p grid, on the device.
+int device_divmax(lh_handle* h, double* out) {
+  CU(h, cudaMemsetAsync(&h->sc->cflbits, 0, sizeof(unsigned long long), h->st));
+  launch_divergence(h->u1, h->u2, h->u3, h->psi, h->d, h->t, h->st);
+  launch_absmax(h->psi, field_elems(h, 'p'), h->sc, h->st);
+  DevScalars s;
+  int rc = read_scalars(h, &s);
+  if (rc) return rc;
+  unsigned long long b = s.cflbits;
+  std::memcpy(out, &b, sizeof(double));
+  CU(h, cudaGetLastError());
+  return LH_OK;
+}
+
 }  // namespace
 
 namespace lh {
+int make_dims(const lh_params* prm, Dims* out, std::string* why) {
+  auto Nf = [&](int row, int band) { return prm->N[band * 4 + row - 1]; };
+  auto Gf = [&](int row, int band) { return prm->Ngal[band * 4 + row - 1]; };
+  auto no = [&](int code, const char* msg) {
+    *why = msg;
+    return code;
+  };
+  Dims d{};
+  d.ngx = Gf(1, 1); d.ngz = Gf(2, 1);
+  const int nx = Nf(1, 1), nz = Nf(2, 1);
+  if (nx != 2 * (d.ngx / 3) || nz != 2 * (d.ngz / 3) || d.ngx < 6 || d.ngz < 6 || (d.ngx & 1) || (nz & 1))
+    return no(LH_EINVAL, "inconsistent N/Ngal");
+  d.nkx = nx / 2 + 1;
+  d.nz = nz;
+  d.np = d.nkx * d.nz;
+  d.mp = d.nkx * d.ngz;
+  d.spitch = d.nkx;
+  d.snz = d.nz;
+  d.ju0 = Nf(4, 0);
+  // variable-resolution bands (start.f90:95-118): the middle band's resolution
+  d.ngx2 = Gf(1, 2); d.ngz2 = Gf(2, 2);
+  d.banded = (d.ngx2 != d.ngx || d.ngz2 != d.ngz);
+  {
+    const int nx2 = Nf(1, 2), nz2 = Nf(2, 2);
+    if (nx2 != 2 * (d.ngx2 / 3) || nz2 != 2 * (d.ngz2 / 3) || d.ngx2 < 6 || d.ngz2 < 6 || (d.ngx2 & 1) || (nz2 & 1) ||
+        d.ngx2 > d.ngx || d.ngz2 > d.ngz || Gf(1, 3) != d.ngx || Gf(2, 3) != d.ngz)
+      return no(LH_EINVAL, "inconsistent band resolutions (the middle band may not be finer than the walls')");
+    d.nkx2 = nx2 / 2 + 1;
+    d.nz2 = nz2;
+  }
+  d.Nu1 = Nf(4, 1) - d.ju0; d.Nu2 = Nf(4, 2) - d.ju0;
+  d.Nv1 = Nf(3, 1) - d.ju0; d.Nv2 = Nf(3, 2) - d.ju0;
+  if (Nf(3, 0) != d.ju0) return no(LH_EINVAL, "N(3,0) != N(4,0)");
+  d.nyu = Nf(4, 3) + 1 - Nf(4, 0) + 1;
+  d.nyv = Nf(3, 3) + 1 - Nf(3, 0) + 1;
+  d.nyp = Nf(4, 3) - (Nf(4, 0) + 1) + 1;
+  d.nn = prm->nn;
+  if (d.nyv != d.nyu - 1 || d.nyp != d.nyu - 2 || d.nyu < 6) return no(LH_EINVAL, "inconsistent y grid sizes");
+  if (d.nn + 2 - d.ju0 >= d.nyu || d.ju0 > 0) return no(LH_EINVAL, "nn outside the u grid");
+  if (d.banded && !(d.Nu1 >= 2 && d.Nv1 == d.Nu1 - 1 && d.Nu2 > d.Nu1 + 1 && d.Nv2 == d.Nu2 && d.Nu2 < d.nyu - 3))
+    return no(LH_EINVAL, "band limits N(3:4,1:2) do not describe three bands");
+  if (!(prm->Re > 0) || !(prm->alp > 0) || !(prm->bet > 0)) return no(LH_EINVAL, "Re, alp, bet must be positive");
+  *out = d;
+  return LH_OK;
+}
+
 void set_init_error(const char* msg) { g_init_error = msg; }
 void set_handle_error(lh_handle* h, const char* msg) {
   if (h) h->err = msg;
@@ -586,6 +657,12 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
   auto Gf = [&](int row, int band) { return prm->Ngal[band * 4 + row - 1]; };
   if (prm->precision != LH_PREC_FP64 && prm->precision != LH_PREC_MIXED) return fail(nullptr, LH_EINVAL, "bad precision");
   if (prm->geometry_type != 0 && prm->geometry_type != 3) return fail(nullptr, LH_EUNSUPPORTED, "geometry_type %d has no forcing builder", prm->geometry_type);
+  Dims dims{};
+  {  // the parameter block is checked before any CUDA call
+    std::string why;
+    const int rc = make_dims(prm, &dims, &why);
+    if (rc) return fail(nullptr, rc, "%s", why.c_str());
+  }
   lh_handle* h = new lh_handle();
   h->prm = *prm;
   h->precision = prm->precision;
@@ -606,41 +683,9 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
     return rc;
   };
   Dims& d = h->d;
-  d.ngx = Gf(1, 1); d.ngz = Gf(2, 1);
+  d = dims;
   const int nx = Nf(1, 1), nz = Nf(2, 1);
-  if (nx != 2 * (d.ngx / 3) || nz != 2 * (d.ngz / 3) || d.ngx < 6 || d.ngz < 6 || (d.ngx & 1) || (nz & 1))
-    return bail(fail(h, LH_EINVAL, "inconsistent N/Ngal"));
-  d.nkx = nx / 2 + 1;
-  d.nz = nz;
-  d.np = d.nkx * d.nz;
-  d.mp = d.nkx * d.ngz;
-  d.spitch = d.nkx;
-  d.snz = d.nz;
-  d.ju0 = Nf(4, 0);
-  // variable-resolution bands (start.f90:95-118): the middle band's resolution
-  d.ngx2 = Gf(1, 2); d.ngz2 = Gf(2, 2);
-  d.banded = (d.ngx2 != d.ngx || d.ngz2 != d.ngz);
-  {
-    const int nx2 = Nf(1, 2), nz2 = Nf(2, 2);
-    if (nx2 != 2 * (d.ngx2 / 3) || nz2 != 2 * (d.ngz2 / 3) || d.ngx2 < 6 || d.ngz2 < 6 || (d.ngx2 & 1) || (nz2 & 1) ||
-        d.ngx2 > d.ngx || d.ngz2 > d.ngz || Gf(1, 3) != d.ngx || Gf(2, 3) != d.ngz)
-      return bail(fail(h, LH_EINVAL, "inconsistent band resolutions (the middle band may not be finer than the walls')"));
-    d.nkx2 = nx2 / 2 + 1;
-    d.nz2 = nz2;
-  }
-  d.Nu1 = Nf(4, 1) - d.ju0; d.Nu2 = Nf(4, 2) - d.ju0;
-  d.Nv1 = Nf(3, 1) - d.ju0; d.Nv2 = Nf(3, 2) - d.ju0;
-  if (Nf(3, 0) != d.ju0) return bail(fail(h, LH_EINVAL, "N(3,0) != N(4,0)"));
-  d.nyu = Nf(4, 3) + 1 - Nf(4, 0) + 1;
-  d.nyv = Nf(3, 3) + 1 - Nf(3, 0) + 1;
-  d.nyp = Nf(4, 3) - (Nf(4, 0) + 1) + 1;
-  d.nn = prm->nn;
-  if (d.nyv != d.nyu - 1 || d.nyp != d.nyu - 2 || d.nyu < 6) return bail(fail(h, LH_EINVAL, "inconsistent y grid sizes"));
-  if (d.nn + 2 - d.ju0 >= d.nyu || d.ju0 > 0) return bail(fail(h, LH_EINVAL, "nn outside the u grid"));
-  if (d.banded && !(d.Nu1 >= 2 && d.Nv1 == d.Nu1 - 1 && d.Nu2 > d.Nu1 + 1 && d.Nv2 == d.Nu2 && d.Nu2 < d.nyu - 3))
-    return bail(fail(h, LH_EINVAL, "band limits N(3:4,1:2) do not describe three bands"));
   h->Re = prm->Re; h->alp = prm->alp; h->bet = prm->bet;
-  if (!(h->Re > 0) || !(h->alp > 0) || !(h->bet > 0)) return bail(fail(h, LH_EINVAL, "Re, alp, bet must be positive"));
   h->Lx = 2.0 * (double)kPi / h->alp;
   h->Lz = 2.0 * (double)kPi / h->bet;
   for (int c = 0; c < 2; ++c)
@@ -900,8 +945,10 @@ int lh_set_fields(lh_handle* h, const double* u1, const double* u2, const double
     double Q;
     if ((rc = host_flowrate(h, &Q))) return rc;
     CU(h, cudaMemcpyAsync(&h->sc->QxT, &Q, sizeof Q, cudaMemcpyHostToDevice, h->st));
-    CU(h, cudaStreamSynchronize(h->st));
   }
+  // new fields: the sticky error bits of the old ones no longer apply
+  CU(h, cudaMemsetAsync(&h->sc->err, 0, sizeof(int), h->st));
+  CU(h, cudaStreamSynchronize(h->st));
   h->have_fields = true;
   return LH_OK;
 }
@@ -1006,17 +1053,66 @@ int lh_rk3_step(lh_handle* h, int32_t nsteps) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) { h->graph = nullptr; return fail(h, LH_ECUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
   }
-  CU(h, cudaEventRecord(h->ev0, h->st));
-  for (int n = 0; n < nsteps; ++n) {
-    CU(h, cudaGraphLaunch(h->graph, h->st));
-    h->t_now += h->dt;
-    h->iter += 1;
+  // steps run in blocks of mon_every (all at once without the monitor); after each block the sticky
+  // non-finite flag of the pressure solve is read, and with the monitor max |div| is checked against maxerr
+  double total_ms = 0.0;
+  for (int done = 0; done < nsteps;) {
+    const int n = h->mon_every > 0 ? std::min(h->mon_every, nsteps - done) : nsteps - done;
+    CU(h, cudaEventRecord(h->ev0, h->st));
+    for (int q = 0; q < n; ++q) CU(h, cudaGraphLaunch(h->graph, h->st));
+    CU(h, cudaEventRecord(h->ev1, h->st));
+    CU(h, cudaEventSynchronize(h->ev1));
+    float ms = 0.f;
+    CU(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    total_ms += ms;
+    done += n;
+    h->t_now += n * h->dt;
+    h->iter += n;
+    h->last_ms = total_ms;
+    int err = 0;
+    int rc = read_err(h, &err);
+    if (rc) return rc;
+    if (err & kErrNonFinite)
+      return fail(h, LH_ENUMERIC, "non-finite value in the fields within steps %lld..%lld", h->iter - n + 1, h->iter);
+    if (h->mon_every > 0) {
+      double dm = 0.0;
+      if ((rc = device_divmax(h, &dm))) return rc;
+      h->last_divmax = dm;
+      if (!(dm <= h->mon_maxerr))
+        return fail(h, LH_ENUMERIC, "max |div| %.3e exceeds maxerr %.3e after step %lld", dm, h->mon_maxerr, h->iter);
+    }
   }
-  CU(h, cudaEventRecord(h->ev1, h->st));
-  CU(h, cudaEventSynchronize(h->ev1));
-  float ms = 0.f;
-  CU(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
-  h->last_ms = ms;
+  if (nsteps == 0) h->last_ms = 0.0;
+  return LH_OK;
+}
+
+int lh_fp64_peak(double* tflops) {
+  if (!tflops) return LH_EINVAL;
+  const double tf = fp64_probe_tflops(nullptr);
+  if (!(tf > 0.0)) return fail(nullptr, LH_ECUDA, "FP64 probe failed");
+  *tflops = tf;
+  return LH_OK;
+}
+
+int lh_set_monitor(lh_handle* h, double maxerr, int32_t every) {
+  if (!h) return LH_EINVAL;
+  if (every < 0) return fail(h, LH_EINVAL, "every < 0");
+  if (every > 0 && !(maxerr >= 0.0)) return fail(h, LH_EINVAL, "maxerr must be non-negative");
+  h->mon_every = every;
+  h->mon_maxerr = maxerr;
+  return LH_OK;
+}
+
+int lh_get_monitor(lh_handle* h, double* divmax, int32_t* err_bits) {
+  if (!h) return LH_EINVAL;
+  cudaSetDevice(h->device);
+  if (divmax) *divmax = h->last_divmax;
+  if (err_bits) {
+    int e = 0;
+    int rc = read_err(h, &e);
+    if (rc) return rc;
+    *err_bits = e;
+  }
   return LH_OK;
 }
 
@@ -1145,6 +1241,15 @@ int lh_ensemble_step(lh_ensemble* e, int32_t nsteps, double* ms) {
     h->t_now += nsteps * h->dt;
     h->iter += nsteps;
   }
+  for (size_t i = 0; i < e->hs.size(); ++i) {
+    int err = 0;
+    if (read_err(e->hs[i], &err)) return ens_fail(e, LH_ECUDA, "reading a member's status failed");
+    if (err & kErrNonFinite) {
+      char msg[128];
+      std::snprintf(msg, sizeof msg, "non-finite value in the fields of member %zu", i);
+      return ens_fail(e, LH_ENUMERIC, msg);
+    }
+  }
   return LH_OK;
 }
 
@@ -1260,16 +1365,7 @@ int lh_profile_step(lh_handle* h, double* ms_by_kind, int32_t* count_by_kind, in
 int lh_divmax(lh_handle* h, double* out) {
   if (!h || !out) return LH_EINVAL;
   cudaSetDevice(h->device);
-  CU(h, cudaMemsetAsync(&h->sc->cflbits, 0, sizeof(unsigned long long), h->st));
-  launch_divergence(h->u1, h->u2, h->u3, h->psi, h->d, h->t, h->st);
-  launch_absmax(h->psi, field_elems(h, 'p'), h->sc, h->st);
-  DevScalars s;
-  int rc = read_scalars(h, &s);
-  if (rc) return rc;
-  unsigned long long b = s.cflbits;
-  std::memcpy(out, &b, sizeof(double));
-  CU(h, cudaGetLastError());
-  return LH_OK;
+  return device_divmax(h, out);
 }
 
 int lh_cfl_dt(lh_handle* h, double cfl, double* dt_out) {
@@ -1328,7 +1424,7 @@ int lh_project(lh_handle* h) {
   CU(h, cudaMemcpyAsync(h->stage, h->p, fp * sizeof(double2), cudaMemcpyDeviceToDevice, h->st));
   const double dtirk = (1.0 / dt) / (h->aRK[0] + h->bRK[0]);
   const double dtrk = dt * (h->aRK[0] + h->bRK[0]);
-  launch_psolve(h->u1, h->u2, h->u3, h->p, h->psi, h->d, h->t, dtirk, dtrk, h->gw[0][0], h->gw[2][1], h->st);
+  launch_psolve(h->u1, h->u2, h->u3, h->p, h->psi, h->d, h->t, dtirk, dtrk, h->gw[0][0], h->gw[2][1], h->sc, h->st);
   CU(h, cudaMemcpyAsync(h->p, h->stage, fp * sizeof(double2), cudaMemcpyDeviceToDevice, h->st));
   CU(h, cudaStreamSynchronize(h->st));
   CU(h, cudaGetLastError());

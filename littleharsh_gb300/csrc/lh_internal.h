@@ -4,7 +4,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "lh_fft.cuh"
+
+struct lh_params;
 
 namespace lh {
 
@@ -98,8 +102,9 @@ struct DevScalars {
   double QxT;    // target flow rate
   double Qx;     // last flow rate seen by the correction
   unsigned long long cflbits;  // max CFL number (bit pattern of a non-negative double)
-  int err;       // sticky error flag
+  int err;       // sticky error bits (kErr*), cleared when fields are uploaded
 };
+constexpr int kErrNonFinite = 1;  // the pressure solve produced a NaN or an infinity
 
 // Transform job for the z passes: nlev planes; plane y of the job reads
 // level (levels ? levels[y] : lev0 + y) of `spec` and uses mix plane y.
@@ -179,8 +184,10 @@ void launch_vsolve(double2* r1, double2* r2, double2* r3, double2* u1, double2* 
 void launch_flowrate(double2* u1, DevScalars* sc, const Dims& d, const Tables& t, int k, double Qx1, cudaStream_t st);
 void launch_build_dg(double* dg2, double* dg3, const double* rows, const Dims& d, const Tables& t, double pin,
                      cudaStream_t st);
+// sc may be NULL; otherwise kErrNonFinite is or-ed into sc->err when a corrected value is not finite
 void launch_psolve(double2* u1, double2* u2, double2* u3, double2* p, double2* psi, const Dims& d,
-                   const Tables& t, double dtirk, double dtrk, double gwb, double gwt, cudaStream_t st);
+                   const Tables& t, double dtirk, double dtrk, double gwb, double gwt, DevScalars* sc,
+                   cudaStream_t st);
 void launch_divergence(const double2* u1, const double2* u2, const double2* u3, double2* div, const Dims& d,
                        const Tables& t, cudaStream_t st);
 void launch_absmax(const double2* x, size_t n, DevScalars* sc, cudaStream_t st);
@@ -204,6 +211,13 @@ void launch_stage_itp(const double2* u2, const double2* u3, double2* vc, double2
                       cudaStream_t st);
 void launch_xcond(const CondArgs& a, const Dims& d, const FftPlan& ph, const double2* rtw, cudaStream_t st);
 cudaError_t configure_kernels();
+// Measured FP64 FMA throughput of the current device in TFLOP/s (FMA = 2 flops), best of three timed
+// launches of a probe kernel; -1 on a CUDA error.  nsm_out (may be NULL) receives the SM count.
+double fp64_probe_tflops(int* nsm_out);
+
+// Grid sizes of a parameter block, with the checks lh_init makes (lh_capi.cu): LH_OK, or an LH_E* code and
+// the reason in *why.
+int make_dims(const ::lh_params* prm, Dims* out, std::string* why);
 
 // Message returned by lh_last_error(NULL) on this thread (lh_capi.cu).
 void set_init_error(const char* msg);

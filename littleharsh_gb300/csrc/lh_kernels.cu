@@ -494,7 +494,9 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
       const double L_x = a1 * um.x + (k2 + a2) * u0.x + a3 * up.x;
       const double L_y = a1 * um.y + (k2 + a2) * u0.y + a3 * up.y;
       const double kf = f == 0 ? kx : kz;
-      const double2 nold = (f == 0 ? a.n1 : a.n3)[c0];
+      // the first substage's zeta is 0 (start.f90:413-427): its old nonlinear term is not read, so a term left
+      // from earlier fields (even a non-finite one) does not enter
+      const double2 nold = a.C2 != 0.0 ? (f == 0 ? a.n1 : a.n3)[c0] : double2{0.0, 0.0};
       double rx = a.C1 * L_x + a.C2 * nold.x + (a.d * kf) * pc.y;
       double ry = a.C1 * L_y + a.C2 * nold.y + -(a.d * kf) * pc.x;
       if (f == 0 && col == 0) rx = rx + (-a.d * a.sc->mpgx);
@@ -530,7 +532,7 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
       const double C3 = -a.d * t.cv[jj];
       const double L_x = a1 * um.x + (k2 + a2) * u0.x + a3 * up.x;
       const double L_y = a1 * um.y + (k2 + a2) * u0.y + a3 * up.y;
-      const double2 nold = a.n2[c0];
+      const double2 nold = a.C2 != 0.0 ? a.n2[c0] : double2{0.0, 0.0};
       double rx = a.C1 * L_x + a.C2 * nold.x + C3 * (p1.x - p0.x);
       double ry = a.C1 * L_y + a.C2 * nold.y + C3 * (p1.y - p0.y);
       const P A = ld(prod<P>(a, 4) + c0), B = ld(prod<P>(a, 5) + c0);
@@ -708,11 +710,16 @@ void launch_build_dg(double* dg2, double* dg3, const double* rows, const Dims& d
 // or one wall band of a short one).  The divergence is formed on the fly in
 // the forward sweep; the backward sweep adds psi to p and corrects u, w on the
 // same levels and v on the faces between them.
+// bit pattern test for a NaN or an infinity (integer work only, off the FP64 pipe)
+__device__ __forceinline__ bool nonfinite(double x) {
+  return ((unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull) == 0x7ff0000000000000ull;
+}
+
 __device__ __forceinline__ void psolve_segment(double2* __restrict__ u1, double2* __restrict__ u2,
                                                double2* __restrict__ u3, double2* __restrict__ p,
                                                double2* __restrict__ psi, const Dims& d, const Tables& t, int col,
                                                double kx, double kz, double dtirk, double dtrk, int lo, int hi,
-                                               bool pin00) {
+                                               bool pin00, bool& bad) {
   // levels are loaded four at a time ahead of the recurrences (the arithmetic and its order are those of
   // one level at a time)
   const size_t np = d.np;
@@ -760,7 +767,10 @@ __device__ __forceinline__ void psolve_segment(double2* __restrict__ u1, double2
                  const double2& vv) {
     const double2 xc = jq == hi ? xn : double2{v.x - b3 * xn.x, v.y - b3 * xn.y};
     const size_t cp = (size_t)jq * np + col, cu = (size_t)(jq + 1) * np + col;
-    p[cp] = double2{pp.x + xc.x, pp.y + xc.y};
+    const double2 pn = double2{pp.x + xc.x, pp.y + xc.y};
+    // a NaN or infinity anywhere in the fields reaches the divergence of its column, hence psi and p
+    bad = bad || nonfinite(pn.x) || nonfinite(pn.y);
+    p[cp] = pn;
     u1[cu] = double2{a.x - (-kxd * xc.y), a.y - (kxd * xc.x)};
     u3[cu] = double2{w.x - (-kzd * xc.y), w.y - (kzd * xc.x)};
     if (jq < hi) {
@@ -795,17 +805,18 @@ __device__ __forceinline__ void psolve_segment(double2* __restrict__ u1, double2
 
 __global__ void __launch_bounds__(128, 4) k_psolve(double2* u1, double2* u2, double2* u3, double2* p, double2* psi,
                                                 Dims d, Tables t, double dtirk, double dtrk, double gwb,
-                                                double gwt) {
+                                                double gwt, DevScalars* sc) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= d.np) return;
   const size_t np = d.np;
   const int i = col % d.nkx, kk = col / d.nkx;
   const double kx = t.kx[i], kz = t.kz[kk];
+  bool bad = false;
   if (is_long(d, i, kk)) {
-    psolve_segment(u1, u2, u3, p, psi, d, t, col, kx, kz, dtirk, dtrk, 0, d.nyp - 1, col == 0);
+    psolve_segment(u1, u2, u3, p, psi, d, t, col, kx, kz, dtirk, dtrk, 0, d.nyp - 1, col == 0, bad);
   } else {
-    psolve_segment(u1, u2, u3, p, psi, d, t, col, kx, kz, dtirk, dtrk, 0, d.Nu1 - 1, false);
-    psolve_segment(u1, u2, u3, p, psi, d, t, col, kx, kz, dtirk, dtrk, d.Nu2, d.nyp - 1, false);
+    psolve_segment(u1, u2, u3, p, psi, d, t, col, kx, kz, dtirk, dtrk, 0, d.Nu1 - 1, false, bad);
+    psolve_segment(u1, u2, u3, p, psi, d, t, col, kx, kz, dtirk, dtrk, d.Nu2, d.nyp - 1, false, bad);
     // v on the end rows of the short column's bands (v_corr, littleharsh.f90:904-905)
     u2[(size_t)(d.Nv1 + 1) * np + col] = double2{0.0, 0.0};
     u2[(size_t)d.Nv2 * np + col] = double2{0.0, 0.0};
@@ -820,12 +831,13 @@ __global__ void __launch_bounds__(128, 4) k_psolve(double2* u1, double2* u2, dou
     u1[(size_t)(d.nyu - 1) * np + col] = double2{-gwt * at.x, -gwt * at.y};
     u3[(size_t)(d.nyu - 1) * np + col] = double2{-gwt * wt.x, -gwt * wt.y};
   }
+  if (bad && sc) atomicOr(&sc->err, kErrNonFinite);
 }
 
 void launch_psolve(double2* u1, double2* u2, double2* u3, double2* p, double2* psi, const Dims& d, const Tables& t,
-                   double dtirk, double dtrk, double gwb, double gwt, cudaStream_t st) {
+                   double dtirk, double dtrk, double gwb, double gwt, DevScalars* sc, cudaStream_t st) {
   dim3 grid((d.np + 127) / 128);
-  k_psolve<<<grid, 128, 0, st>>>(u1, u2, u3, p, psi, d, t, dtirk, dtrk, gwb, gwt);
+  k_psolve<<<grid, 128, 0, st>>>(u1, u2, u3, p, psi, d, t, dtirk, dtrk, gwb, gwt, sc);
 }
 
 __global__ void k_divergence(const double2* u1, const double2* u2, const double2* u3, double2* div, Dims d, Tables t) {
@@ -1132,6 +1144,57 @@ void launch_spectra(const double2* u1, const double2* u2, const double2* u3, con
                     const Dims& d, const Tables& t, cudaStream_t st) {
   dim3 grid((d.np + 255) / 256, d.nyu);
   k_spectra<<<grid, 256, 0, st>>>(u1, u2, u3, p, sp, d, t);
+}
+
+// FP64 FMA throughput probe: every thread runs eight independent dependent
+// chains of fma(x, a, b), enough independent work to keep the FP64 pipe busy;
+// the sum is stored only if it equals an impossible value, so no chain is
+// removed by the compiler.
+__global__ void __launch_bounds__(256) k_fp64_probe(double* out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) x[q] = 1e-9 * threadIdx.x + q;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) x[q] = fma(x[q], a, b);
+  }
+  double sum = 0.0;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) sum += x[q];
+  if (sum == -1.0) out[blockIdx.x] = sum;
+}
+
+double fp64_probe_tflops(int* nsm_out) {
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return -1.0;
+  if (nsm_out) *nsm_out = nsm;
+  const int blocks = nsm * 8, threads = 256, iters = 4096;
+  double* out = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  double best = -1.0;
+  if (cudaMalloc(&out, sizeof(double) * blocks) == cudaSuccess && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess &&
+      cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
+    k_fp64_probe<<<blocks, threads, 0, st>>>(out, iters / 8, 0.9999999, 1e-7);  // warm-up
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(e0, st);
+      k_fp64_probe<<<blocks, threads, 0, st>>>(out, iters, 0.9999999, 1e-7);
+      cudaEventRecord(e1, st);
+      if (cudaEventSynchronize(e1) != cudaSuccess) { best = -1.0; break; }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+      const double tf = flops / (ms * 1e-3) / 1e12;
+      if (tf > best) best = tf;
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  if (out) cudaFree(out);
+  if (cudaGetLastError() != cudaSuccess) return -1.0;
+  return best;
 }
 
 // Opt the transform kernels in to the largest dynamic shared memory the

@@ -20,7 +20,6 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <string>
 #include <vector>
 
@@ -34,9 +33,6 @@ namespace {
 constexpr size_t kNoAllocScratchBytes = 64ull << 20;
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kMaxDevices = 128;
-std::mutex g_mu;
-void* g_scratch_addr[kMaxDevices] = {};
 // Failures are reported through lh_last_error(NULL).
 int na_fail(int code, const char* fmt, ...) {
   char buf[512];
@@ -50,20 +46,14 @@ int na_fail(int code, const char* fmt, ...) {
 
 // Device address of the scratch array on the current device.  The name of a
 // __device__ array is only a host-side stand-in, so the address is looked up
-// once per device with that device current.
+// with that device current, on every call: a cached address would go stale
+// after cudaDeviceReset, which unloads the module.  The lookup is cheap next
+// to the solve.
 int scratch_address(unsigned char** out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return na_fail(LH_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return na_fail(LH_EUNSUPPORTED, "device %d out of range", dev);
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return na_fail(LH_ECUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-    g_scratch_addr[dev] = p;
-  }
-  *out = static_cast<unsigned char*>(g_scratch_addr[dev]);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return na_fail(LH_ECUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+  *out = static_cast<unsigned char*>(p);
   return LH_OK;
 }
 
@@ -77,29 +67,15 @@ extern "C" int lh_project_noalloc(const lh_params* prm, const double* yu, const 
   if (!prm || !yu || !dthdyu || !dthdyv || !u1 || !u2 || !u3) return na_fail(LH_EINVAL, "NULL argument");
   if (prm->abi_version != LH_ABI_VERSION) return na_fail(LH_EINVAL, "abi_version %d", prm->abi_version);
   if (!(dt > 0.0)) return na_fail(LH_EINVAL, "dt must be positive");
-  auto Nf = [&](int row, int band) { return prm->N[band * 4 + row - 1]; };
-  auto Gf = [&](int row, int band) { return prm->Ngal[band * 4 + row - 1]; };
-  if (Gf(1, 1) != Gf(1, 2) || Gf(2, 1) != Gf(2, 2))
-    return na_fail(LH_EUNSUPPORTED, "bands with different x/z resolutions are not built");
+  // the checks lh_init makes on the parameter block
   Dims d{};
-  d.ngx = Gf(1, 1);
-  d.ngz = Gf(2, 1);
-  const int nx = Nf(1, 1), nz = Nf(2, 1);
-  if (nx != 2 * (d.ngx / 3) || nz != 2 * (d.ngz / 3) || nx < 4 || nz < 4 || (nz & 1))
-    return na_fail(LH_EINVAL, "inconsistent N/Ngal");
-  d.nkx = nx / 2 + 1;
-  d.nz = nz;
-  d.np = d.nkx * nz;
-  d.mp = d.nkx * d.ngz;
-  d.spitch = d.nkx;
-  d.snz = nz;
-  d.ju0 = Nf(4, 0);
-  d.nyu = Nf(4, 3) + 1 - Nf(4, 0) + 1;
-  d.nyv = Nf(3, 3) + 1 - Nf(3, 0) + 1;
-  d.nyp = Nf(4, 3) - (Nf(4, 0) + 1) + 1;
-  d.nn = prm->nn;
-  if (d.nyv != d.nyu - 1 || d.nyp != d.nyu - 2 || d.nyu < 6 || d.ju0 > 0 || 2 - d.ju0 >= d.nyu)
-    return na_fail(LH_EINVAL, "inconsistent y grid sizes");
+  {
+    std::string why;
+    const int rc = make_dims(prm, &d, &why);
+    if (rc) return na_fail(rc, "%s", why.c_str());
+  }
+  if (d.banded) return na_fail(LH_EUNSUPPORTED, "bands with different x/z resolutions are not built");
+  const int nz = d.nz;
   // scratch layout
   const size_t np = (size_t)d.np, nyp = (size_t)d.nyp;
   const size_t o_kx = 0, o_kz = o_kx + up256(8 * (size_t)d.nkx), o_k2x = o_kz + up256(8 * (size_t)nz),
@@ -166,7 +142,7 @@ extern "C" int lh_project_noalloc(const lh_params* prm, const double* yu, const 
   const double dtirk = (1.0 / dt) / ab, dtrk = dt * ab;
   const double gwb = prm->gridweighting[0], gwt = prm->gridweighting[3 + 2];  // gridweighting(1,1), (3,2)
   launch_psolve(reinterpret_cast<double2*>(u1), reinterpret_cast<double2*>(u2), reinterpret_cast<double2*>(u3), p,
-                psi, d, t, dtirk, dtrk, gwb, gwt, st);
+                psi, d, t, dtirk, dtrk, gwb, gwt, nullptr, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return na_fail(LH_ECUDA, "launch: %s", cudaGetErrorString(e));
   e = cudaStreamSynchronize(st);

@@ -62,12 +62,14 @@ def test_three_substages_sequence(oracle_mod):
         _cmp_fields(o, s, SUBSTAGE_TOL, f"after kRK={k}")
 
 
-@pytest.mark.parametrize("cfg", [SMALL, C1], ids=["canopy24", "config1_96x97"])
-def test_ten_steps_fp64(oracle_mod, cfg):
+@pytest.mark.parametrize("cfg,nsteps", [(SMALL, 10), (C1, 10), (C1, 100)],
+                         ids=["canopy24", "config1_96x97", "config1_96x97_100steps"])
+def test_ten_steps_fp64(oracle_mod, cfg, nsteps):
+    """10 RK3 steps within 1e-10 (the target's bound); configuration 1 also over its stated 100-step run."""
     o, s = _pair(oracle_mod, cfg)
-    o.step(10)
-    s.step(10)
-    _cmp_fields(o, s, STEP10_TOL, "10 steps")
+    o.step(nsteps)
+    s.step(nsteps)
+    _cmp_fields(o, s, STEP10_TOL, f"{nsteps} steps")
     assert abs(s.time()["mpgx"] - o.scalars()["mpgx"]) < 1e-9 * abs(o.scalars()["mpgx"])
     assert s.divmax() < 1e-9
 
