@@ -47,7 +47,8 @@
 extern "C" {
 #endif
 
-#define LH_ABI_VERSION 1
+/* 2: lh_stats_flush fills rows 11-12 (omega_x) and lh_cond_flush returns 13 blocks */
+#define LH_ABI_VERSION 2
 
 enum {
   LH_OK = 0,
@@ -177,10 +178,16 @@ int lh_spectra_flush(lh_handle* h, double* spU, double* spV, double* spW, double
 
 /* Plane statistics (stats.f90:1-108), FP64 sums over the physical planes of
  * each level: out is 13 x max(nyu, nyv): Um U2m Vm V2m Wm W2m Pm P2m UVm UWm
- * VWm (rows 11-12, omega_x, are reserved and stay zero).  Rows on the v or p
- * grid use their first nyv / nyp entries.  UVm pairs u with v interpolated to
- * the centres, VWm v with w interpolated to the faces (both zero on ghost
- * centres / wall faces).  The sums are formed from the spectral coefficients
+ * VWm wxm wx2m.  Rows on the v or p grid use their first nyv / nyp entries.
+ * UVm pairs u with v interpolated to the centres, VWm v with w interpolated to
+ * the faces (both zero on ghost centres / wall faces).  wxm, wx2m are the
+ * streamwise vorticity omega_x = dw/dy - dv/dz on every face, the y-difference
+ * of w across the face with the pressure gradient's metric dthdyv
+ * (littleharsh.f90:685) minus i kz v (the routine that fills the reference's
+ * wx, in FOU3D.f90, is missing).  Every row sums the whole plane; the
+ * reference's wx loop covers only i <= N(1), k <= N(2) of its Ngal-sized wx
+ * array (stats.f90:53-58), bounds left from an earlier N-grid allocation
+ * (start.f90:637-638).  The sums are formed from the spectral coefficients
  * (Parseval on the 3/2 grid), equal to the physical sums up to rounding.
  * Call between steps: it reuses the right-hand-side scratch. */
 int lh_stats_accumulate(lh_handle* h);
@@ -193,9 +200,11 @@ int lh_stats_flush(lh_handle* h, double* out, int32_t* count, int32_t reset);
  * from the top wall with v's sign flipped (write_stats sums the two,
  * stats.f90:473-512), accumulated in FP64 from physical planes.  dims[0..4] =
  * nju, njv, njp, dnx, dnz (nju = N(4,1)-N(4,0)+1, njv = N(3,1)-N(3,0)+1,
- * njp = N(4,1)-N(4,0)-1; all 0 without canopies).  out: 11 blocks
+ * njp = N(4,1)-N(4,0)-1; all 0 without canopies).  out: 13 blocks
  * [j1][kin][i] (i fastest): UmC U2mC WmC W2mC UVmC UWmC (nju planes), VmC
- * V2mC VWmC (njv), PmC P2mC (njp).  Call between steps. */
+ * V2mC VWmC (njv), PmC P2mC (njp), wxmC wx2mC (njv; omega_x keeps its sign on
+ * the top wall, as condup1 is called with xsign = 1 for wx, stats.f90:102).
+ * Call between steps. */
 int lh_cond_accumulate(lh_handle* h);
 int lh_cond_flush(lh_handle* h, double* out, int32_t* dims5, int32_t* count, int32_t reset);
 

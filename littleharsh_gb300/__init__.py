@@ -24,7 +24,7 @@ __all__ = ["Solver", "Config", "Input", "read_input", "load_library", "LhError",
 
 PREC_FP64, PREC_MIXED = 0, 1
 LAYOUT_PLANES, LAYOUT_COLUMNS = 0, 1
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 EXPORTED_SYMBOLS = [
     "lh_init", "lh_free", "lh_last_error", "lh_get_sizes", "lh_set_fields", "lh_get_fields", "lh_set_nonlinear",
@@ -378,7 +378,7 @@ class Solver:
     def project(self):
         self._check(load_library().lh_project(self.h))
 
-    STAT_ROWS = ("Um", "U2m", "Vm", "V2m", "Wm", "W2m", "Pm", "P2m", "UVm", "UWm", "VWm")
+    STAT_ROWS = ("Um", "U2m", "Vm", "V2m", "Wm", "W2m", "Pm", "P2m", "UVm", "UWm", "VWm", "wxm", "wx2m")
 
     def stats_accumulate(self):
         self._check(load_library().lh_stats_accumulate(self.h))
@@ -390,10 +390,11 @@ class Solver:
         n = C.c_int32(0)
         self._check(load_library().lh_stats_flush(self.h, _p(o), C.byref(n), int(reset)))
         ny = dict(Um=self.nyu, U2m=self.nyu, Vm=self.nyv, V2m=self.nyv, Wm=self.nyu, W2m=self.nyu, Pm=self.nyp,
-                  P2m=self.nyp, UVm=self.nyu, UWm=self.nyu, VWm=self.nyv)
+                  P2m=self.nyp, UVm=self.nyu, UWm=self.nyu, VWm=self.nyv, wxm=self.nyv, wx2m=self.nyv)
         return n.value, {k: o[r, :ny[k]].copy() for r, k in enumerate(self.STAT_ROWS)}
 
-    COND_ROWS = ("UmC", "U2mC", "WmC", "W2mC", "UVmC", "UWmC", "VmC", "V2mC", "VWmC", "PmC", "P2mC")
+    COND_ROWS = ("UmC", "U2mC", "WmC", "W2mC", "UVmC", "UWmC", "VmC", "V2mC", "VWmC", "PmC", "P2mC", "wxmC",
+                 "wx2mC")
 
     def cond_accumulate(self):
         self._check(load_library().lh_cond_accumulate(self.h))
@@ -405,7 +406,7 @@ class Solver:
         n = C.c_int32(0)
         self._check(L.lh_cond_flush(self.h, None, dims.ctypes.data, C.byref(n), 0))
         nju, njv, njp, dnx, dnz = [int(x) for x in dims]
-        sizes = [nju] * 6 + [njv] * 3 + [njp] * 2
+        sizes = [nju] * 6 + [njv] * 3 + [njp] * 2 + [njv] * 2
         out = np.zeros(max(sum(sizes) * dnx * dnz, 1))
         self._check(L.lh_cond_flush(self.h, _p(out), dims.ctypes.data, C.byref(n), int(reset)))
         res, off = {}, 0

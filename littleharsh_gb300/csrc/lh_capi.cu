@@ -886,7 +886,7 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
       for (int j = 0; j < h->njp; ++j) { pl[2 * j] = j; pl[2 * j + 1] = d.nyp - 1 - j; }
       const size_t tile = (size_t)h->dnx * h->dnz;
       if ((rc = upload(h, &h->cond_ul, ul)) || (rc = upload(h, &h->cond_vl, vl)) || (rc = upload(h, &h->cond_pl, pl)) ||
-          (rc = dalloc(h, &h->cond, tile * (6 * (size_t)h->nju + 3 * (size_t)h->njv + 2 * (size_t)h->njp))))
+          (rc = dalloc(h, &h->cond, tile * (6 * (size_t)h->nju + 5 * (size_t)h->njv + 2 * (size_t)h->njp))))
         return bail(rc);
     }
   }
@@ -1474,8 +1474,8 @@ int lh_stats_accumulate(lh_handle* h) {
   if (!h) return LH_EINVAL;
   if (!h->have_fields) return fail(h, LH_ESTATE, "fields must be set first");
   cudaSetDevice(h->device);
-  // v at centres and w at faces are staged in the right-hand-side buffers, which are dead between steps
-  launch_stats(h->u1, h->u2, h->u3, h->p, h->r1, h->r3, h->stat, h->d, h->t, h->st);
+  // v at centres, w and omega_x at faces are staged in the right-hand-side buffers, which are dead between steps
+  launch_stats(h->u1, h->u2, h->u3, h->p, h->r1, h->r3, h->r2, h->stat, h->d, h->t, h->st);
   CU(h, cudaGetLastError());
   h->nstat += 1;
   return LH_OK;
@@ -1488,16 +1488,17 @@ int lh_cond_accumulate(lh_handle* h) {
   cudaSetDevice(h->device);
   const Dims& d = h->d;
   cudaStream_t st = h->st;
-  // v at centres and w at faces staged in the right-hand-side scratch (dead between steps)
-  launch_stage_itp(h->u2, h->u3, h->r1, h->r3, d, h->t, st);
-  // the FP64 mixed planes of one chunk live in the substage's mixed buffers: 2 planes (both walls) per j1
+  // v at centres, w and omega_x at faces staged in the right-hand-side scratch (dead between steps)
+  launch_stage_itp(h->u2, h->u3, h->r1, h->r3, h->r2, d, h->t, st);
+  // the FP64 mixed planes of one chunk live in the substage's mixed buffers: 2 planes (both walls) per j1; the
+  // smallest of them (uv products) holds nyv planes of the handle's precision
   const size_t cb = h->precision == LH_PREC_MIXED ? sizeof(float2) : sizeof(double2);
-  const int cap = (int)((size_t)d.nyu * cb / (2 * sizeof(double2)));
+  const int cap = (int)((size_t)d.nyv * cb / (2 * sizeof(double2)));
   if (cap < 1) return fail(h, LH_EINVAL, "no room for the conditional statistics planes");
   const size_t tile = (size_t)h->dnx * h->dnz;
   const int njmax = std::max(h->nju, std::max(h->njv, h->njp));
-  double2* mx[6] = {(double2*)h->mixu, (double2*)h->mixw, (double2*)h->mixp[0], (double2*)h->mixp[1],
-                    (double2*)h->mixp[2], (double2*)h->mixp[3]};
+  double2* mx[7] = {(double2*)h->mixu, (double2*)h->mixw, (double2*)h->mixp[0], (double2*)h->mixp[1],
+                    (double2*)h->mixp[2], (double2*)h->mixp[3], (double2*)h->mixp[4]};
   for (int j0 = 0; j0 < njmax; j0 += cap) {
     const int cu = std::max(0, std::min(cap, h->nju - j0)), cvv = std::max(0, std::min(cap, h->njv - j0)),
               cp = std::max(0, std::min(cap, h->njp - j0));
@@ -1508,16 +1509,18 @@ int lh_cond_accumulate(lh_handle* h) {
     J.j[3] = ZJob<double>{h->u2, nullptr, mx[3], h->cond_vl + 2 * j0, 0, 2 * cvv};
     J.j[4] = ZJob<double>{h->r3, nullptr, mx[4], h->cond_vl + 2 * j0, 0, 2 * cvv};
     J.j[5] = ZJob<double>{h->p, nullptr, mx[5], h->cond_pl + 2 * j0, 0, 2 * cp};
-    J.njobs = 6;
+    J.j[6] = ZJob<double>{h->r2, nullptr, mx[6], h->cond_vl + 2 * j0, 0, 2 * cvv};
+    J.njobs = 7;
     J.maxlev = 2 * std::max(cu, std::max(cvv, cp));
     launch_zinv<double>(J, d, h->pz.plan, h->tx, st);
     CondArgs a{};
     a.mix[0][0] = mx[0]; a.mix[0][1] = mx[1]; a.mix[0][2] = mx[2];
-    a.mix[1][0] = mx[3]; a.mix[1][1] = mx[4];
+    a.mix[1][0] = mx[3]; a.mix[1][1] = mx[4]; a.mix[1][2] = mx[6];
     a.mix[2][0] = mx[5];
     a.out[0] = h->cond;
     a.out[1] = h->cond + 6 * (size_t)h->nju * tile;
     a.out[2] = a.out[1] + 3 * (size_t)h->njv * tile;
+    a.outw = a.out[2] + 2 * (size_t)h->njp * tile;
     a.nj[0] = cu; a.nj[1] = cvv; a.nj[2] = cp;
     a.njtot[0] = h->nju; a.njtot[1] = h->njv; a.njtot[2] = h->njp;
     a.j0 = j0;
@@ -1535,7 +1538,7 @@ int lh_cond_flush(lh_handle* h, double* out, int32_t* dims, int32_t* count, int3
   if (dims) { dims[0] = h->nju; dims[1] = h->njv; dims[2] = h->njp; dims[3] = h->dnx; dims[4] = h->dnz; }
   if (count) *count = h->ncond;
   if (!h->cond) return LH_OK;
-  const size_t n = (size_t)h->dnx * h->dnz * (6 * (size_t)h->nju + 3 * (size_t)h->njv + 2 * (size_t)h->njp);
+  const size_t n = (size_t)h->dnx * h->dnz * (6 * (size_t)h->nju + 5 * (size_t)h->njv + 2 * (size_t)h->njp);
   if (out) CU(h, cudaMemcpyAsync(out, h->cond, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   if (reset) {
     CU(h, cudaMemsetAsync(h->cond, 0, n * sizeof(double), h->st));

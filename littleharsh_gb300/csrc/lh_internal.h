@@ -196,19 +196,24 @@ void launch_transpose(const double2* src, double2* dst, int rows, int cols, cuda
 void launch_gather_col(const double2* src, size_t stride, int n, double2* dst, cudaStream_t st);
 void launch_spectra(const double2* u1, const double2* u2, const double2* u3, const double2* p, double* sp,
                     const Dims& d, const Tables& t, cudaStream_t st);
+// vc, wf: nyu and nyv staging planes; om: nyv staging planes (omega_x)
 void launch_stats(const double2* u1, const double2* u2, const double2* u3, const double2* p, double2* vc,
-                  double2* wf, double* acc, const Dims& d, const Tables& t, cudaStream_t st);
+                  double2* wf, double2* om, double* acc, const Dims& d, const Tables& t, cudaStream_t st);
 // Conditional statistics pass over one chunk of wall-band planes (grids g: 0 u, 1 v, 2 p).
 struct CondArgs {
-  const double2* mix[3][3];  // mixed planes per grid and field (u: u, w, v at centres; v: v, w at faces; p: p)
+  const double2* mix[3][3];  // mixed planes per grid and field (u: u, w, v at centres; v: v, w, omega_x at faces;
+                             // p: p)
   double* out[3];            // accumulators per grid: [quantity][j1][kin][i]
+  double* outw;              // the v grid's omega_x accumulators: [2][j1][kin][i]
   int nj[3];                 // planes of this chunk per grid
   int njtot[3];              // planes per grid in total
   int j0;                    // first j1 of the chunk
   int dnx, dnz, ntx, ntz;
 };
-void launch_stage_itp(const double2* u2, const double2* u3, double2* vc, double2* wf, const Dims& d, const Tables& t,
-                      cudaStream_t st);
+// v at every centre and w at every face (zero on ghost centres and wall faces); om (may be NULL): omega_x at
+// every face
+void launch_stage_itp(const double2* u2, const double2* u3, double2* vc, double2* wf, double2* om, const Dims& d,
+                      const Tables& t, cudaStream_t st);
 void launch_xcond(const CondArgs& a, const Dims& d, const FftPlan& ph, const double2* rtw, cudaStream_t st);
 cudaError_t configure_kernels();
 // Measured FP64 FMA throughput of the current device in TFLOP/s (FMA = 2 flops), best of three timed

@@ -191,7 +191,7 @@ int lh_read_restart(lh_handle* h, const char* dir, const char* name, double* t_o
 // write_stats (stats.f90:355-410): header, Ngal, (yu, dthetai, dthdyu), (yv, dthetai, dthdyv), istat, the 13
 // plane profiles (Um U2m Vm V2m Wm W2m Pm P2m UVm UWm VWm wxm wx2m) and, with canopies, the 13 conditional
 // blocks (UmC U2mC VmC V2mC WmC W2mC PmC P2mC UVmC UWmC VWmC wxmC wx2mC), then resets the accumulators as
-// write_stats does.  The omega_x records are written as zeros (not accumulated).
+// write_stats does.
 int lh_write_stats(lh_handle* h, const lh_params* prm, const double* yu, const double* yv, const double* dthdyu,
                    const double* dthdyv, const char* path, int32_t iter) {
   if (!h || !prm || !yu || !yv || !dthdyu || !dthdyv || !path) return LH_EINVAL;
@@ -205,7 +205,7 @@ int lh_write_stats(lh_handle* h, const lh_params* prm, const double* yu, const d
   int32_t istat = 0, dims[5] = {0, 0, 0, 0, 0}, nc = 0;
   if ((rc = lh_cond_flush(h, nullptr, dims, &nc, 0))) return rc;
   const size_t tile = (size_t)dims[3] * dims[4];
-  std::vector<double> cond(tile * (6 * (size_t)dims[0] + 3 * (size_t)dims[1] + 2 * (size_t)dims[2]) + 1);
+  std::vector<double> cond(tile * (6 * (size_t)dims[0] + 5 * (size_t)dims[1] + 2 * (size_t)dims[2]) + 1);
   if ((rc = lh_cond_flush(h, cond.data(), dims, &nc, 1))) return rc;
   if ((rc = lh_stats_flush(h, st.data(), &istat, 1))) return rc;
   double tm[5];
@@ -220,23 +220,21 @@ int lh_write_stats(lh_handle* h, const lh_params* prm, const double* yu, const d
   w.record({{yu, 8 * (size_t)s.nyu}, {&dthetai, 8}, {dthdyu, 8 * (size_t)s.nyu}});
   w.record({{yv, 8 * (size_t)s.nyv}, {&dthetai, 8}, {dthdyv, 8 * (size_t)s.nyv}});
   w.record({{&istat, 4}});
-  // device rows: 0 Um 1 U2m 2 Vm 3 V2m 4 Wm 5 W2m 6 Pm 7 P2m 8 UVm 9 UWm 10 VWm; written in that order, then wx
-  const int ny_of[11] = {s.nyu, s.nyu, s.nyv, s.nyv, s.nyu, s.nyu, s.nyp, s.nyp, s.nyu, s.nyu, s.nyv};
-  for (int r = 0; r < 11; ++r) w.record({{st.data() + (size_t)r * L, 8 * (size_t)ny_of[r]}});
-  std::vector<double> zeros((size_t)(s.nyv > 0 ? s.nyv : 1), 0.0);
-  w.record({{zeros.data(), 8 * (size_t)s.nyv}});
-  w.record({{zeros.data(), 8 * (size_t)s.nyv}});
+  // device rows: 0 Um 1 U2m 2 Vm 3 V2m 4 Wm 5 W2m 6 Pm 7 P2m 8 UVm 9 UWm 10 VWm 11 wxm 12 wx2m, written in that
+  // order (recvX, stats.f90:369-382)
+  const int ny_of[13] = {s.nyu, s.nyu, s.nyv, s.nyv, s.nyu, s.nyu, s.nyp, s.nyp, s.nyu, s.nyu, s.nyv, s.nyv, s.nyv};
+  for (int r = 0; r < 13; ++r) w.record({{st.data() + (size_t)r * L, 8 * (size_t)ny_of[r]}});
   if (tile) {
-    // device block order: UmC U2mC WmC W2mC UVmC UWmC | VmC V2mC VWmC | PmC P2mC
+    // device block order: UmC U2mC WmC W2mC UVmC UWmC | VmC V2mC VWmC | PmC P2mC | wxmC wx2mC
     const size_t bu = tile * dims[0], bv = tile * dims[1], bp = tile * dims[2];
     const double* c = cond.data();
     const double *UmC = c, *U2mC = c + bu, *WmC = c + 2 * bu, *W2mC = c + 3 * bu, *UVmC = c + 4 * bu, *UWmC = c + 5 * bu;
     const double *VmC = c + 6 * bu, *V2mC = VmC + bv, *VWmC = VmC + 2 * bv;
     const double *PmC = VmC + 3 * bv, *P2mC = PmC + bp;
-    std::vector<double> zc(bv > 0 ? bv : 1, 0.0);
+    const double *wxmC = P2mC + bp, *wx2mC = wxmC + bv;
     const std::pair<const double*, size_t> recs[13] = {{UmC, bu}, {U2mC, bu}, {VmC, bv}, {V2mC, bv}, {WmC, bu},
                                                        {W2mC, bu}, {PmC, bp}, {P2mC, bp}, {UVmC, bu}, {UWmC, bu},
-                                                       {VWmC, bv}, {zc.data(), bv}, {zc.data(), bv}};
+                                                       {VWmC, bv}, {wxmC, bv}, {wx2mC, bv}};
     for (const auto& rr : recs) w.record({{rr.first, 8 * rr.second}});
   }
   if (!w.ok) return io_fail(LH_EINVAL, std::string("write failed: ") + path);

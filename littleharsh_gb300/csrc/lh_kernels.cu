@@ -946,7 +946,8 @@ __global__ void k_spectra(const double2* u1, const double2* u2, const double2* u
 // makes it (its imaginary part is dropped; the lone kz = -N2/2 mode splits
 // into -N2/2 and +N2/2 on the padded grid).  sum f = Ngx Ngz Re f(0,0).
 // acc rows (length L = max(nyu, nyv)): 0 Um 1 U2m 2 Vm 3 V2m 4 Wm 5 W2m 6 Pm 7 P2m
-// 8 UVm (u, v at centres) 9 UWm 10 VWm (v, w at faces).  One block per level.
+// 8 UVm (u, v at centres) 9 UWm 10 VWm (v, w at faces) 11 wxm 12 wx2m (omega_x
+// at faces, omega_at_face below).  One block per level.
 // With bands a plane of the middle band sums over its own points: only the long
 // columns count, the lone mode is that band's -N2/2 and the factor its Ngx Ngz.
 __device__ __forceinline__ double pair_term(const double2* f, const double2* g, int col, int i, int kk, int nz,
@@ -960,19 +961,33 @@ __device__ __forceinline__ double pair_term(const double2* f, const double2* g, 
   return 0.5 * (re + (a.x * c.x - a.y * c.y));  // + Re(a g(-kz))
 }
 
+// Streamwise vorticity omega_x = dw/dy - dv/dz at face jj of column col (the wx
+// planes of stats.f90:53-58,93,102, filled in the reference by the missing
+// FOU3D.f90): the y-difference of w across the face with the pressure
+// gradient's metric (littleharsh.f90:685) minus i kz v.
+__device__ __forceinline__ double2 omega_at_face(const double2* u2, const double2* u3, const Dims& d, const Tables& t,
+                                                 int jj, int col) {
+  const size_t np = d.np;
+  const double c = t.cv[jj], kz = t.kz[col / d.nkx];
+  const double2 w0 = u3[(size_t)jj * np + col], w1 = u3[(size_t)(jj + 1) * np + col], v = u2[(size_t)jj * np + col];
+  return double2{c * (w1.x - w0.x) + kz * v.y, c * (w1.y - w0.y) - kz * v.x};
+}
+
 __global__ void __launch_bounds__(256) k_stats(const double2* u1, const double2* u2, const double2* u3,
-                                               const double2* p, double2* vc, double2* wf, double* acc, Dims d,
-                                               Tables t, int L) {
+                                               const double2* p, double2* vc, double2* wf, double2* om, double* acc,
+                                               Dims d, Tables t, int L) {
   const int jj = blockIdx.x;
   const size_t np = d.np;
-  double s[11];
+  double s[13];
 #pragma unroll
-  for (int r = 0; r < 11; ++r) s[r] = 0.0;
-  // v at the centre jj and w at the face jj (zero on ghost centres and wall faces)
+  for (int r = 0; r < 13; ++r) s[r] = 0.0;
+  // v at the centre jj, w at the face jj (zero on ghost centres and wall faces) and omega_x at the face jj
   double2* vcl = vc + (size_t)blockIdx.x * np;
   double2* wfl = wf + (size_t)blockIdx.x * np;
+  double2* oml = om + (size_t)blockIdx.x * np;
   const bool cin = jj >= 1 && jj <= d.nyu - 2, fin = jj >= 1 && jj <= d.nyv - 2;
   for (int col = threadIdx.x; col < d.np; col += blockDim.x) {
+    if (jj < d.nyv) oml[col] = omega_at_face(u2, u3, d, t, jj, col);
     double2 v = double2{0.0, 0.0}, w = double2{0.0, 0.0};
     if (cin) {
       const double2 v0 = u2[(size_t)(jj - 1) * np + col], v1 = u2[(size_t)jj * np + col];
@@ -1009,42 +1024,44 @@ __global__ void __launch_bounds__(256) k_stats(const double2* u1, const double2*
       const int lone = cv_ ? lone_c : lone_f;
       s[3] += pair_term(V, V, col, i, kk, d.nz, d.nkx, lone);
       s[10] += pair_term(V, wfl, col, i, kk, d.nz, d.nkx, lone);
+      s[12] += pair_term(oml, oml, col, i, kk, d.nz, d.nkx, lone);
     }
     if (jj < d.nyp && (lng || !cp_)) s[7] += pair_term(P, P, col, i, kk, d.nz, d.nkx, cp_ ? lone_c : lone_f);
   }
   if (threadIdx.x == 0) {
     if (jj < d.nyu) { s[0] = U[0].x; s[4] = W[0].x; }
-    if (jj < d.nyv) s[2] = V[0].x;
+    if (jj < d.nyv) { s[2] = V[0].x; s[11] = oml[0].x; }
     if (jj < d.nyp) s[6] = P[0].x;
   }
-  __shared__ double red[8][11];
+  __shared__ double red[8][13];
 #pragma unroll
-  for (int r = 0; r < 11; ++r) {
+  for (int r = 0; r < 13; ++r) {
     double x = s[r];
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][r] = x;
   }
   __syncthreads();
-  if (threadIdx.x < 11) {
+  if (threadIdx.x < 13) {
     double x = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) x += red[w][threadIdx.x];
     const int r = threadIdx.x;
-    const bool coarse = (r == 2 || r == 3 || r == 10) ? cv_ : ((r == 6 || r == 7) ? cp_ : cu_);
+    const bool coarse = (r == 2 || r == 3 || r >= 10) ? cv_ : ((r == 6 || r == 7) ? cp_ : cu_);
     const double scale = coarse ? (double)d.ngx2 * (double)d.ngz2 : (double)d.ngx * (double)d.ngz;
     acc[(size_t)r * L + jj] += scale * x;
   }
 }
 
 void launch_stats(const double2* u1, const double2* u2, const double2* u3, const double2* p, double2* vc,
-                  double2* wf, double* acc, const Dims& d, const Tables& t, cudaStream_t st) {
+                  double2* wf, double2* om, double* acc, const Dims& d, const Tables& t, cudaStream_t st) {
   const int L = d.nyu > d.nyv ? d.nyu : d.nyv;
-  k_stats<<<L, 256, 0, st>>>(u1, u2, u3, p, vc, wf, acc, d, t, L);
+  k_stats<<<L, 256, 0, st>>>(u1, u2, u3, p, vc, wf, om, acc, d, t, L);
 }
 
 // v interpolated to every centre and w to every face in spectral space (zero
 // on ghost centres and wall faces): the y interpolation the statistics pair
 // u with v and v with w through.
-__global__ void k_stage_itp(const double2* u2, const double2* u3, double2* vc, double2* wf, Dims d, Tables t) {
+__global__ void k_stage_itp(const double2* u2, const double2* u3, double2* vc, double2* wf, double2* om, Dims d,
+                            Tables t) {
   const int col = blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= d.np) return;
   const int jj = blockIdx.y;
@@ -1066,13 +1083,14 @@ __global__ void k_stage_itp(const double2* u2, const double2* u3, double2* vc, d
       w = double2{w0.x + c * (w1.x - w0.x), w0.y + c * (w1.y - w0.y)};
     }
     wf[c0] = w;
+    if (om) om[c0] = omega_at_face(u2, u3, d, t, jj, col);
   }
 }
 
-void launch_stage_itp(const double2* u2, const double2* u3, double2* vc, double2* wf, const Dims& d, const Tables& t,
-                      cudaStream_t st) {
+void launch_stage_itp(const double2* u2, const double2* u3, double2* vc, double2* wf, double2* om, const Dims& d,
+                      const Tables& t, cudaStream_t st) {
   dim3 grid((d.np + 255) / 256, d.nyu);
-  k_stage_itp<<<grid, 256, 0, st>>>(u2, u3, vc, wf, d, t);
+  k_stage_itp<<<grid, 256, 0, st>>>(u2, u3, vc, wf, om, d, t);
 }
 
 // Conditional statistics (conddown1/2, condup1/2: stats.f90:110-253; both
@@ -1090,8 +1108,8 @@ __global__ void __launch_bounds__(128) k_xcond(CondArgs a, Dims d, FftPlan ph, c
   const int g = blockIdx.z, jl = blockIdx.x, kin = blockIdx.y;
   const int nj = a.nj[g];
   if (jl >= nj) return;
-  const int nf = g == 0 ? 3 : (g == 1 ? 2 : 1);
-  const int nq = g == 0 ? 6 : (g == 1 ? 3 : 2);
+  const int nf = g == 2 ? 1 : 3;
+  const int nq = g == 0 ? 6 : (g == 1 ? 5 : 2);
   for (int e = threadIdx.x; e < 6 * a.dnx; e += blockDim.x) acc[e] = 0.0;
   __syncthreads();
   for (int iz = 0; iz < a.ntz; ++iz) {
@@ -1112,8 +1130,9 @@ __global__ void __launch_bounds__(128) k_xcond(CondArgs a, Dims d, FftPlan ph, c
             const double B = rows[ngx + x], C = rows[2 * ngx + x];
             q[0] += A; q[1] += A * A; q[2] += B; q[3] += B * B; q[4] += A * (sg * C); q[5] += A * B;
           } else if (g == 1) {
-            const double B = rows[ngx + x];
-            q[0] += sg * A; q[1] += A * A; q[2] += (sg * A) * B;
+            // omega_x keeps its sign on the top wall (condup1 called with xsign = 1 for wx, stats.f90:102)
+            const double B = rows[ngx + x], C = rows[2 * ngx + x];
+            q[0] += sg * A; q[1] += A * A; q[2] += (sg * A) * B; q[3] += C; q[4] += C * C;
           } else {
             q[0] += A; q[1] += A * A;
           }
@@ -1126,7 +1145,10 @@ __global__ void __launch_bounds__(128) k_xcond(CondArgs a, Dims d, FftPlan ph, c
   const size_t pl = (size_t)a.dnx * a.dnz;
   for (int i = threadIdx.x; i < a.dnx; i += blockDim.x)
     for (int r = 0; r < nq; ++r) {
-      double* o = a.out[g] + (size_t)r * a.njtot[g] * pl + (size_t)(a.j0 + jl) * pl + (size_t)kin * a.dnx + i;
+      // the v grid's omega_x sums (quantities 3, 4) have their own blocks after the p grid's
+      double* base = (g == 1 && r >= 3) ? a.outw + (size_t)(r - 3) * a.njtot[1] * pl
+                                        : a.out[g] + (size_t)r * a.njtot[g] * pl;
+      double* o = base + (size_t)(a.j0 + jl) * pl + (size_t)kin * a.dnx + i;
       *o += acc[r * a.dnx + i];
     }
 }

@@ -816,7 +816,7 @@ lho* lho_create(const lho_config* cfg, char* err, int errlen) {
     s->njv = N[2][1] - N[2][0] + 1;
     s->njp = N[3][1] - N[3][0] - 1;
     const size_t pl = (size_t)s->dnx * s->dnz;
-    s->cond = (double*)xcalloc(pl * (6 * (size_t)s->nju + 3 * (size_t)s->njv + 2 * (size_t)s->njp), 8);
+    s->cond = (double*)xcalloc(pl * (6 * (size_t)s->nju + 5 * (size_t)s->njv + 2 * (size_t)s->njp), 8);
   }
   return s;
 }
@@ -1551,6 +1551,27 @@ static void v_to_centres(const lho* s, double* out) {
   }
 }
 
+/* Streamwise vorticity omega_x = dw/dy - dv/dz on every face of the v grid
+ * (the wx planes of stats.f90:53-58,93,102; the routine that fills wx lives in
+ * the missing FOU3D.f90).  In spectral space per column:
+ * wx(face j) = ddthetavi*dthdyv(j)*(w(centre j+1) - w(centre j)) - i kz v(face j),
+ * the y-difference across the face with the metric of the pressure gradient
+ * (littleharsh.f90:685). */
+static void omega_x(const lho* s, double* out) {
+  const int nc = s->nplane, nkx = s->nkx;
+  for (int jj = 0; jj < s->nyv; ++jj) {
+    const int j = jj + s->jv0;
+    const double c = s->ddthetavi * DTHV(s, j);
+    const size_t f = 2 * (size_t)jj * nc, c0 = 2 * (size_t)(j - s->ju0) * nc, c1 = c0 + 2 * (size_t)nc;
+    for (int col = 0; col < nc; ++col) {
+      const double kz = s->kz[col / nkx];
+      const size_t q = 2 * (size_t)col;
+      out[f + q] = c * (s->u3[c1 + q] - s->u3[c0 + q]) + kz * s->u2[f + q + 1];
+      out[f + q + 1] = c * (s->u3[c1 + q + 1] - s->u3[c0 + q + 1]) - kz * s->u2[f + q];
+    }
+  }
+}
+
 void lho_spectra_accumulate(lho* s) {
   const int nc = s->nplane;
   double* vi = (double*)xcalloc(2 * (size_t)s->nyu * nc, 8);
@@ -1580,14 +1601,19 @@ void lho_spectra_get(const lho* s, double* spU, double* spV, double* spW, double
 /* Profiles, stored as 13 rows of length nyu (rows on the v or p grid use the
  * first nyv / nyp entries): 0 Um, 1 U2m, 2 Vm, 3 V2m, 4 Wm, 5 W2m, 6 Pm, 7 P2m,
  * 8 UVm (u grid, v interpolated to centres), 9 UWm (u grid), 10 VWm (v grid,
- * w interpolated to faces), 11/12 reserved (omega_x, not accumulated). */
+ * w interpolated to faces), 11 wxm, 12 wx2m (v grid, omega_x above).  The
+ * reference's wx loop runs over i <= N(1), k <= N(2) of its Ngal-sized wx
+ * array, bounds left from an earlier N-grid allocation (start.f90:637-638);
+ * here every plane statistic, wx's included, sums the whole physical plane. */
 void lho_stats_accumulate(lho* s) {
   const int nc = s->nplane, ngx = s->ngx, ngz = s->ngz;
   const size_t PL = (size_t)ngx * ngz;
   const int L = s->nyu > s->nyv ? s->nyu : s->nyv;
   double* vi = (double*)xcalloc(2 * (size_t)s->nyu * nc, 8);
   double* wi = (double*)xcalloc(2 * (size_t)s->nyv * nc, 8);
+  double* ox = (double*)xcalloc(2 * (size_t)s->nyv * nc, 8);
   v_to_centres(s, vi);
+  omega_x(s, ox);
   for (int jj = 1; jj < s->nyv - 1; ++jj) {
     const int j = jj + s->jv0;
     const double wf = (YV(s, j) - YU(s, j)) / (YU(s, j + 1) - YU(s, j));
@@ -1620,6 +1646,8 @@ void lho_stats_accumulate(lho* s) {
         plane_to_phys_r(s, r, s->u2 + 2 * (size_t)jj * nc, A, scr);
         plane_to_phys_r(s, r, wi + 2 * (size_t)jj * nc, B, scr);
         for (size_t n = 0; n < P; ++n) { acc[2] += A[n]; acc[3] += A[n] * A[n]; acc[10] += A[n] * B[n]; }
+        plane_to_phys_r(s, r, ox + 2 * (size_t)jj * nc, A, scr);
+        for (size_t n = 0; n < P; ++n) { acc[11] += A[n]; acc[12] += A[n] * A[n]; }
       }
       if (jj < s->nyp) {
         const int r = res_u(s, jj + s->jp0);
@@ -1632,7 +1660,7 @@ void lho_stats_accumulate(lho* s) {
     free(scr); free(A); free(B);
   }
   s->istat++;
-  free(vi); free(wi);
+  free(vi); free(wi); free(ox);
 }
 
 int lho_stats_get(const lho* s, double* out) {
@@ -1647,8 +1675,10 @@ int lho_stats_get(const lho* s, double* out) {
  * p: N(4,0)+1+j1) plus the top band's planes counted from the top wall
  * (u: N(4,3)+1-j1, v: N(3,3)+1-j1, p: N(4,3)-j1) with v's sign flipped.
  * Each entry sums a field over the ntilex x ntilez tiles at one in-tile point.
- * Layout of lho_cond_get's output: 11 blocks [j1][kin][i] (i fastest):
- * UmC U2mC WmC W2mC UVmC UWmC (nju planes), VmC V2mC VWmC (njv), PmC P2mC (njp). */
+ * Layout of lho_cond_get's output: 13 blocks [j1][kin][i] (i fastest):
+ * UmC U2mC WmC W2mC UVmC UWmC (nju planes), VmC V2mC VWmC (njv), PmC P2mC (njp),
+ * wxmC wx2mC (njv; omega_x with sign +1 on both walls, as condup1 is called
+ * with xsign = 1 for wx at stats.f90:102). */
 void lho_cond_accumulate(lho* s) {
   if (!s->cond) return;
   const int nc = s->nplane, ngx = s->ngx, ngz = s->ngz, dnx = s->dnx, dnz = s->dnz;
@@ -1656,7 +1686,9 @@ void lho_cond_accumulate(lho* s) {
   const size_t PL = (size_t)ngx * ngz, pl = (size_t)dnx * dnz;
   double* vi = (double*)xcalloc(2 * (size_t)s->nyu * nc, 8);
   double* wi = (double*)xcalloc(2 * (size_t)s->nyv * nc, 8);
+  double* ox = (double*)xcalloc(2 * (size_t)s->nyv * nc, 8);
   v_to_centres(s, vi);
+  omega_x(s, ox);
   for (int jj = 1; jj < s->nyv - 1; ++jj) {
     const int j = jj + s->jv0;
     const double wf = (YV(s, j) - YU(s, j)) / (YU(s, j + 1) - YU(s, j));
@@ -1664,10 +1696,10 @@ void lho_cond_accumulate(lho* s) {
     for (size_t n = 0; n < 2 * (size_t)nc; ++n)
       wi[2 * (size_t)jj * nc + n] = s->u3[c0 + n] + wf * (s->u3[c1 + n] - s->u3[c0 + n]);
   }
-  double* blk[11];
+  double* blk[13];
   blk[0] = s->cond;
-  for (int q = 1; q < 11; ++q) {
-    const int nj = q <= 6 ? s->nju : (q <= 9 ? s->njv : s->njp);  /* size of block q-1 */
+  for (int q = 1; q < 13; ++q) {
+    const int nj = q <= 6 ? s->nju : (q <= 9 ? s->njv : (q <= 11 ? s->njp : s->njv));  /* size of block q-1 */
     blk[q] = blk[q - 1] + (size_t)nj * pl;
   }
   const size_t sl = plane_scratch_len(s);
@@ -1698,15 +1730,18 @@ void lho_cond_accumulate(lho* s) {
       const int jv = side ? s->nyv - 1 - j1 : j1;
       plane_to_phys_(s, s->u2 + 2 * (size_t)jv * nc, A, scr);
       plane_to_phys_(s, wi + 2 * (size_t)jv * nc, B, scr);
+      plane_to_phys_(s, ox + 2 * (size_t)jv * nc, C, scr);
       for (int k = 0; k < dnz; ++k)
         for (int i = 0; i < dnx; ++i) {
-          double a[3] = {0, 0, 0};
+          double a[5] = {0, 0, 0, 0, 0};
           for (int iz = 0; iz < tz; ++iz)
             for (int ix = 0; ix < tx; ++ix) {
               const size_t n = (size_t)(k + dnz * iz) * ngx + i + dnx * ix;
               a[0] += sg * A[n]; a[1] += A[n] * A[n]; a[2] += (sg * A[n]) * B[n];
+              a[3] += C[n]; a[4] += C[n] * C[n];
             }
           for (int q = 0; q < 3; ++q) blk[6 + q][(size_t)j1 * pl + (size_t)k * dnx + i] += a[q];
+          for (int q = 0; q < 2; ++q) blk[11 + q][(size_t)j1 * pl + (size_t)k * dnx + i] += a[3 + q];
         }
     }
     for (int j1 = 0; j1 < s->njp; ++j1) {
@@ -1724,17 +1759,17 @@ void lho_cond_accumulate(lho* s) {
         }
     }
   }
-  free(scr); free(A); free(B); free(C); free(vi); free(wi);
+  free(scr); free(A); free(B); free(C); free(vi); free(wi); free(ox);
   s->icond++;
 }
 
-/* out: the 11 blocks described above; returns the number of accumulations.
+/* out: the 13 blocks described above; returns the number of accumulations.
  * dims[0..4] = nju, njv, njp, dnx, dnz (all 0 without canopies). */
 int lho_cond_get(const lho* s, double* out, int32_t* dims) {
   if (dims) { dims[0] = s->nju; dims[1] = s->njv; dims[2] = s->njp; dims[3] = s->dnx; dims[4] = s->dnz; }
   if (out && s->cond) {
     const size_t pl = (size_t)s->dnx * s->dnz;
-    memcpy(out, s->cond, 8 * pl * (6 * (size_t)s->nju + 3 * (size_t)s->njv + 2 * (size_t)s->njp));
+    memcpy(out, s->cond, 8 * pl * (6 * (size_t)s->nju + 5 * (size_t)s->njv + 2 * (size_t)s->njp));
   }
   return s->icond;
 }

@@ -274,7 +274,8 @@ class Oracle:
     def spectra_accumulate(self):
         lib().lho_spectra_accumulate(self.h)
 
-    COND_ROWS = ("UmC", "U2mC", "WmC", "W2mC", "UVmC", "UWmC", "VmC", "V2mC", "VWmC", "PmC", "P2mC")
+    COND_ROWS = ("UmC", "U2mC", "WmC", "W2mC", "UVmC", "UWmC", "VmC", "V2mC", "VWmC", "PmC", "P2mC", "wxmC",
+                 "wx2mC")
 
     def cond_accumulate(self):
         lib().lho_cond_accumulate(self.h)
@@ -284,7 +285,7 @@ class Oracle:
         dims = np.zeros(5, np.int32)
         lib().lho_cond_get(self.h, None, dims.ctypes.data)
         nju, njv, njp, dnx, dnz = [int(x) for x in dims]
-        sizes = [nju] * 6 + [njv] * 3 + [njp] * 2
+        sizes = [nju] * 6 + [njv] * 3 + [njp] * 2 + [njv] * 2
         out = np.zeros(sum(sizes) * dnx * dnz)
         n = lib().lho_cond_get(self.h, _p(out) if out.size else None, dims.ctypes.data)
         res, off = {}, 0

@@ -74,7 +74,7 @@ def test_band_statistics(oracle_mod):
     no, so = o.stats()
     assert n == no == 1
     ny = {"u": s.nyu, "v": s.nyv, "p": s.nyp}
-    for r, (name, grid) in enumerate(zip(s.STAT_ROWS, "uuvvuuppuuv")):
+    for r, (name, grid) in enumerate(zip(s.STAT_ROWS, "uuvvuuppuuvvv")):
         a, b = st[name], so[r, :ny[grid]]
         tol = 1e-11 * np.abs(b).max() + 1e-13 * s.ngx * s.ngz
         assert np.abs(a - b).max() < tol, f"{name}: {np.abs(a - b).max():.3e} >= {tol:.3e}"

@@ -80,12 +80,14 @@ def test_stats_file(oracle_mod, tmp_path):
     assert len(recs) == 5 + 13 + 13
     np.testing.assert_array_equal(np.frombuffer(recs[1], np.int32), np.array(s.params.Ngal, np.int32))
     assert np.frombuffer(recs[4], np.int32)[0] == 1
-    names = ["Um", "U2m", "Vm", "V2m", "Wm", "W2m", "Pm", "P2m", "UVm", "UWm", "VWm"]
+    names = ["Um", "U2m", "Vm", "V2m", "Wm", "W2m", "Pm", "P2m", "UVm", "UWm", "VWm", "wxm", "wx2m"]
     for k, name in enumerate(names):
         np.testing.assert_array_equal(np.frombuffer(recs[5 + k], np.float64), st[name])
-    cnames = ["UmC", "U2mC", "VmC", "V2mC", "WmC", "W2mC", "PmC", "P2mC", "UVmC", "UWmC", "VWmC"]
+    cnames = ["UmC", "U2mC", "VmC", "V2mC", "WmC", "W2mC", "PmC", "P2mC", "UVmC", "UWmC", "VWmC", "wxmC", "wx2mC"]
     for k, name in enumerate(cnames):
         np.testing.assert_array_equal(np.frombuffer(recs[18 + k], np.float64), cd[name].ravel())
+    # the omega_x records hold the accumulated vorticity (not zeros)
+    assert np.abs(st["wx2m"]).max() > 0 and np.abs(cd["wx2mC"]).max() > 0
     # write_stats resets the accumulators
     assert s.stats_flush()[0] == 0 and s.cond_flush()[0] == 0
 

@@ -137,7 +137,7 @@ def test_plane_statistics(oracle_mod):
     no, so = o.stats()
     assert n == no == 2
     ny = {"u": s.nyu, "v": s.nyv, "p": s.nyp}
-    for r, (name, grid) in enumerate(zip(s.STAT_ROWS, "uuvvuuppuuv")):
+    for r, (name, grid) in enumerate(zip(s.STAT_ROWS, "uuvvuuppuuvvv")):
         a, b = st[name], so[r, :ny[grid]]
         # means of v vanish by continuity: an absolute floor of 1e-13 per summed point covers round-off
         tol = 1e-11 * np.abs(b).max() + 1e-13 * s.ngx * s.ngz

@@ -134,3 +134,27 @@ def test_plane_sums_by_parseval(oracle_mod):
     assert abs((pf * pg).sum() - _parseval_sum(f, g, o.ngx, o.ngz)) < 1e-12 * abs((pf * pg).sum()) + 1e-10
     assert abs((pf * pf).sum() - _parseval_sum(f, f, o.ngx, o.ngz)) < 1e-12 * (pf * pf).sum()
     assert abs(pf.sum() - o.ngx * o.ngz * f[0, 0].real) < 1e-10
+
+
+def test_omega_x_statistics_from_the_spectra(oracle_mod):
+    """The oracle's omega_x rows (wxm, wx2m) against an evaluation from the spectral coefficients alone:
+    omega_x(face j) = dthdyv(j) (w(centre j+1) - w(centre j)) - i kz v(face j) per mode; its plane sum is
+    Ngx Ngz Re omega(0,0) and its sum of squares Ngx Ngz times Parseval's sum (kx > 0 twice, the Hermitian kx = 0
+    line once; the field has no lone -N2/2 mode)."""
+    from tests.helpers import projected_ic
+    o = oracle_mod.Oracle(**SMALL)
+    u1, u2, u3, p = projected_ic(o, seed=9)
+    o.set_fields(u1, u2, u3, p)
+    o.stats_accumulate()
+    n, st = o.stats()
+    assert n == 1
+    g = o.grid()
+    kz = 2.0 * np.where(np.arange(o.nz) < o.nz // 2, np.arange(o.nz), np.arange(o.nz) - o.nz)
+    om = g["dthdyv"][:, None, None] * (u3[1:] - u3[:-1]) - 1j * kz[None, :, None] * u2
+    pts = o.ngx * o.ngz
+    mean = pts * om[:, 0, 0].real
+    sq = pts * (2.0 * np.sum(np.abs(om[:, :, 1:]) ** 2, axis=(1, 2)) + np.sum(np.abs(om[:, :, 0]) ** 2, axis=1))
+    nyv = o.nyv
+    assert np.abs(st[11, :nyv] - mean).max() < 1e-11 * np.abs(mean).max() + 1e-12 * pts
+    assert np.abs(st[12, :nyv] - sq).max() < 1e-11 * sq.max()
+    assert sq.max() > 0
