@@ -70,5 +70,24 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+DRIVER_SRC = os.path.join(PKG, "driver", "lh_driver.c")
+
+
+def build_driver(out: str | None = None) -> str:
+    """Compile the C host driver (littleharsh_gb300/driver/lh_driver.c) against include/littleharsh.h and link
+    it to the library; returns the executable's path (default: next to the library)."""
+    lib = build()
+    exe = out or os.path.join(OUT_DIR, "lh_driver")
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        raise RuntimeError("no C compiler found")
+    cmd = [cc, "-O2", "-std=c99", "-Wall", "-Wextra", "-I" + os.path.join(ROOT, "include"), DRIVER_SRC, "-o", exe,
+           "-L" + OUT_DIR, "-llh_gb300", "-Wl,-rpath," + OUT_DIR]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0 or not os.path.exists(lib):
+        raise RuntimeError(f"driver build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return exe
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))
