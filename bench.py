@@ -291,36 +291,55 @@ def _config(args, cfg: dict, world: int) -> dict:
 
 
 def run_ensemble(args, rank: int, world: int):
+    """Configuration 4: 16 replicas of uneven sizes advanced together from one graph per step with one stream per
+    replica (the ensemble's default mode, the line's value), beside batched launches (one per kernel kind,
+    substage slot and grid class) and the replicas one by one, each with its own graph; the same start and steps
+    in every mode."""
     import littleharsh_gb300 as lh
     cfgs = ensemble_configs()
     prec = lh.PREC_MIXED if args.precision == "mixed" else lh.PREC_FP64
     members = [build_solver(c, prec, seed=100 + i)[0] for i, c in enumerate(cfgs)]
     pts = sum(m.ngx * m.ngz * m.nyu for m in members)
-    e = lh.Ensemble(members)
-    e.step(max(args.warmup, 1))
-    sampler = ClockSampler(0)
-    sampler.start()
-    ms = e.step(args.steps)
-    clocks = sampler.stop()
-    # the same replicas one by one, each with its own graph
+    start = [m.get_fields() for m in members]
+    times = [m.time() for m in members]
+
+    def reset():
+        for m, f, t in zip(members, start, times):
+            m.set_fields(*f)
+            m.set_time(t["t"], t["dt"], t["mpgx"], t["QxT"])
+    res = {}
+    for mode, name in ((lh.ENS_BATCHED, "batched"), (lh.ENS_STREAMS, "streams")):
+        reset()
+        e = lh.Ensemble(members, mode=mode)
+        e.step(max(args.warmup, 1))
+        sampler = ClockSampler(0)
+        sampler.start()
+        ms = e.step(args.steps)
+        clocks = sampler.stop()
+        res[name] = {"ms_per_step": ms / args.steps, "value": pts * args.steps / (ms / 1e3), "clocks": clocks,
+                     **e.info()}
+        e.close()
+    reset()
     for m in members:
-        m.step(1)
+        m.step(max(args.warmup, 1))
     seq = 0.0
     for m in members:
         m.step(args.steps)
         seq += m.last_step_ms()[0]
-    value = pts * args.steps / (ms / 1e3)
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if prec == lh.PREC_FP64 else "mixed f32/f64",
+    b = res["streams"]
+    line = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": b["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if prec == lh.PREC_FP64 else "mixed f32/f64",
             "data": "synthetic (seeded laminar + 10% perturbation, projected divergence-free)",
             "config": {"workload": "ensemble16_config4", "replicas": len(members),
                        "grids": sorted({(m.ngx, m.ngz, m.nyu) for m in members}), "precision": args.precision},
-            "sequential": {"value": pts * args.steps / (seq / 1e3), "ms_per_step": seq / args.steps},
-            "speedup_vs_sequential": seq / ms, "gpu_launches": sum(m.last_step_ms()[1] for m in members) * args.steps,
-            "clocks": clocks}
+            "batched": b, "streams": res["streams"],
+            "sequential": {"value": pts * args.steps / (seq / 1e3), "ms_per_step": seq / args.steps,
+                           "launches_per_step": sum(m.last_step_ms()[1] for m in members)},
+            "speedup_vs_sequential": (seq / args.steps) / b["ms_per_step"],
+            "batched_vs_streams": res["streams"]["ms_per_step"] / res["batched"]["ms_per_step"],
+            "gpu_launches": b["launches_per_step"] * args.steps, "clocks": b["clocks"]}
     print(json.dumps(line), flush=True)
-    e.close()
     for m in members:
         m.close()
 

@@ -210,12 +210,30 @@ int lh_cond_flush(lh_handle* h, double* out, int32_t* dims5, int32_t* count, int
 
 /* Ensembles of independent replicas (uneven grids and geometries allowed) on
  * one device: lh_ensemble_step advances every member by nsteps RK3 steps with
- * one CUDA-graph launch per step; the graph forks into each member's stream,
- * so the members' kernels run concurrently.  Members keep their own state and
- * can still be used alone.  ms (may be NULL) receives the device time.  No
- * counterpart in the reference (one simulation per MPI job). */
+ * one CUDA-graph launch per step.  Members keep their own state and can still
+ * be used alone.  ms (may be NULL) receives the device time.  No counterpart
+ * in the reference (one simulation per MPI job), whose per-replica loop is
+ * the main loop itself (littleharsh.f90:161-201).
+ * Modes (lh_ensemble_set_mode):
+ *   LH_ENS_STREAMS (default)  the graph forks into each member's stream,
+ *     each member launching its own kernels, so the members' kernels overlap.
+ *   LH_ENS_BATCHED  one launch per kernel kind and slot of the substage
+ *     (each band's z-inverse, product pass and z-forward, assembly, canopy
+ *     forcing, Thomas sweeps, flow rate, pressure solve) for every grid class
+ *     (members with the same grid) and shared-memory size, covering the
+ *     blocks of all its members, with the members' arguments in the launch's
+ *     kernel parameter (up to 32 members per launch); the classes' launches
+ *     run on streams of their own.  The launches per step do not grow with
+ *     the member count.  Needs members of one precision; otherwise the
+ *     streams mode is used.
+ * Either way each member's arithmetic is that of its own lh_rk3_step, bit for
+ * bit.  lh_ensemble_info reports the mode of the captured graph and its
+ * kernel launches per step. */
+enum { LH_ENS_STREAMS = 0, LH_ENS_BATCHED = 1 };
 int lh_ensemble_create(lh_handle* const* members, int32_t n, lh_ensemble** out);
+int lh_ensemble_set_mode(lh_ensemble* e, int32_t mode);
 int lh_ensemble_step(lh_ensemble* e, int32_t nsteps, double* ms);
+int lh_ensemble_info(const lh_ensemble* e, int32_t* mode_used, int32_t* launches_per_step);
 const char* lh_ensemble_last_error(const lh_ensemble* e);
 void lh_ensemble_free(lh_ensemble* e);
 

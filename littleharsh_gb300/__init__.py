@@ -32,7 +32,7 @@ EXPORTED_SYMBOLS = [
     "lh_cfl_dt", "lh_project", "lh_spectra_accumulate", "lh_spectra_flush", "lh_stats_accumulate",
     "lh_stats_flush", "lh_cond_accumulate", "lh_cond_flush", "lh_last_step_ms", "lh_profile_step",
     "lh_project_noalloc", "lh_set_monitor", "lh_get_monitor", "lh_fp64_peak", "lh_ensemble_create", "lh_ensemble_step", "lh_ensemble_last_error",
-    "lh_ensemble_free", "lh_autotune", "lh_get_launch_shapes", "lh_write_restart", "lh_read_restart", "lh_write_stats", "lh_write_spectra", "lh_read_input", "lh_setup_grid", "lh_setup_canopy",
+    "lh_ensemble_free", "lh_ensemble_set_mode", "lh_ensemble_info", "lh_autotune", "lh_get_launch_shapes", "lh_write_restart", "lh_read_restart", "lh_write_stats", "lh_write_spectra", "lh_read_input", "lh_setup_grid", "lh_setup_canopy",
     # include/lh_srnet.h: kernels of the learned warm start
     "lh_sr_conv_fwd", "lh_sr_conv_fwd_tc", "lh_sr_tc_status", "lh_sr_conv_wgrad", "lh_sr_flip_weights", "lh_sr_mse", "lh_sr_adam",
 ]
@@ -139,6 +139,8 @@ def load_library(build: bool = True) -> C.CDLL:
     L.lh_ensemble_last_error.restype = cp
     L.lh_ensemble_free.argtypes = [vp]
     L.lh_ensemble_free.restype = None
+    L.lh_ensemble_set_mode.argtypes = [vp, i32]
+    L.lh_ensemble_info.argtypes = [vp, C.POINTER(i32), C.POINTER(i32)]
     L.lh_read_input.argtypes = [cp, C.POINTER(Input)]
     L.lh_setup_grid.argtypes = [C.POINTER(Input), C.POINTER(Params)] + [_dp] * 6
     L.lh_setup_canopy.argtypes = [C.POINTER(Input), C.POINTER(Params), C.c_void_p, C.POINTER(i32), C.c_void_p,
@@ -450,25 +452,42 @@ class Solver:
         return n.value, o
 
 
-class Ensemble:
-    """Independent solvers advanced together, one CUDA graph launch per RK3 step."""
+ENS_STREAMS, ENS_BATCHED = 0, 1
 
-    def __init__(self, members):
+
+class Ensemble:
+    """Independent solvers advanced together, one CUDA graph launch per RK3 step: one stream per member (the
+    default) or batched launches (one per kernel kind, substage slot and grid class, covering its members)."""
+
+    def __init__(self, members, mode: int = ENS_STREAMS):
         self.members = list(members)
         L = load_library()
         arr = (C.c_void_p * len(self.members))(*[m.h.value for m in self.members])
         e = C.c_void_p()
         rc = L.lh_ensemble_create(arr, len(self.members), C.byref(e))
         if rc:
-            raise LhError(f"lh_ensemble_create failed ({rc}): {L.lh_last_error(None).decode()}")
+            raise LhError(f"lh_ensemble_create failed ({rc}): {L.lh_last_error(None).decode()}", rc)
         self.e = e
+        self.set_mode(mode)
+
+    def set_mode(self, mode: int):
+        L = load_library()
+        rc = L.lh_ensemble_set_mode(self.e, mode)
+        if rc:
+            raise LhError(f"lh_ensemble_set_mode failed ({rc}): {L.lh_ensemble_last_error(self.e).decode()}", rc)
+
+    def info(self) -> dict:
+        """Mode of the captured graph and its kernel launches per step."""
+        m, n = C.c_int32(0), C.c_int32(0)
+        load_library().lh_ensemble_info(self.e, C.byref(m), C.byref(n))
+        return {"mode": "batched" if m.value == ENS_BATCHED else "streams", "launches_per_step": n.value}
 
     def step(self, n: int = 1) -> float:
         ms = C.c_double(0)
         L = load_library()
         rc = L.lh_ensemble_step(self.e, n, C.byref(ms))
         if rc:
-            raise LhError(f"lh_ensemble_step failed ({rc}): {L.lh_ensemble_last_error(self.e).decode()}")
+            raise LhError(f"lh_ensemble_step failed ({rc}): {L.lh_ensemble_last_error(self.e).decode()}", rc)
         return ms.value
 
     def close(self):

@@ -343,12 +343,19 @@ int band_launches(const lh_handle* h, BandLaunch* out) {
   return 3;
 }
 
-// The nonlinear term's plane work, one band at a time (one band without
-// variable resolution): z-inverse of the levels the band's products need,
-// products, z-forward of the band's product planes.  The flags select parts
-// (the autotuner times them separately); a substage runs all three.
+// The nonlinear term's plane work for one band: z-inverse of the levels the band's products need, products,
+// z-forward of the band's product planes, with the geometry and transforms of the band's planes.
 template <typename R>
-void enqueue_nonlinear(lh_handle* h, cudaStream_t st, bool zinv, bool xprod, bool zfwd) {
+struct NlBand {
+  const Dims* d;
+  const FftPlan *pz, *ph, *pf;
+  const double2* rtw;
+  ZJobs<R> zi, zf;
+  ProdArgs<R> xp;
+};
+
+template <typename R>
+int nl_bands(const lh_handle* h, NlBand<R>* out) {
   using T2 = cpx_t<R>;
   const Dims& d = h->d;
   BandLaunch bl[3];
@@ -356,20 +363,24 @@ void enqueue_nonlinear(lh_handle* h, cudaStream_t st, bool zinv, bool xprod, boo
   for (int b = 0; b < nbl; ++b) {
     const BandLaunch& B = bl[b];
     const Dims& db = *B.d;
+    NlBand<R>& o = out[b];
+    o.d = B.d; o.pz = B.pz; o.ph = B.ph; o.pf = B.pf; o.rtw = B.rtw;
     const int L0 = std::min(B.c_lo, B.f_lo + 1), L1 = std::max(B.c_hi, B.f_hi + 1);
-    if (zinv) {
+    {
       const int ul = std::max(1, L0 - 1), uh = std::min(d.nyu - 2, L1);
       const int vl = std::max(1, L0 - 1), vh = std::min(d.nyv - 2, L1);
       ZJobs<R> J{};
       J.j[0] = ZJob<R>{h->u1, nullptr, (T2*)h->mixu + (size_t)ul * db.mp, nullptr, ul, uh - ul + 1};
       J.j[1] = ZJob<R>{h->u3, nullptr, (T2*)h->mixw + (size_t)ul * db.mp, nullptr, ul, uh - ul + 1};
       J.j[2] = ZJob<R>{h->u2, nullptr, (T2*)h->mixv + (size_t)vl * db.mp, nullptr, vl, std::max(0, vh - vl + 1)};
+      // the mixed form transforms the fluctuations of u and w; the product pass adds the level means back
+      // outside the FP32 transforms (ProdArgs::mean_split)
+      J.j[0].nomean = J.j[1].nomean = sizeof(R) == 4;
       J.njobs = 3;
       J.maxlev = uh - ul + 1;
-      launch_zinv<R>(J, db, *B.pz, h->tx, st);
-      mark(h, K_ZINV);
+      o.zi = J;
     }
-    if (xprod) {
+    {
       ProdArgs<R> a{};
       a.mu = (const T2*)h->mixu;
       a.mw = (const T2*)h->mixw;
@@ -379,10 +390,11 @@ void enqueue_nonlinear(lh_handle* h, cudaStream_t st, bool zinv, bool xprod, boo
       a.dxi = db.ngx / h->Lx; a.dzi = db.ngz / h->Lz;
       a.sc = h->sc; a.want_cfl = 0; a.chunk = h->chunk; a.split = h->xsplit;
       a.c_lo = B.c_lo; a.c_hi = B.c_hi; a.f_lo = B.f_lo; a.f_hi = B.f_hi;
-      launch_xprod<R>(a, db, *B.ph, *B.pf, B.rtw, st);
-      mark(h, K_XPROD);
+      a.mean_split = sizeof(R) == 4;
+      a.us = h->u1; a.ws = h->u3; a.nps = d.np;
+      o.xp = a;
     }
-    if (zfwd) {
+    {
       ZJobs<R> J{};
       double2* outs[6] = {h->puu, h->puw, h->pww, h->pvv, h->puv, h->pvw};
       for (int i = 0; i < 6; ++i) {
@@ -392,7 +404,31 @@ void enqueue_nonlinear(lh_handle* h, cudaStream_t st, bool zinv, bool xprod, boo
       }
       J.njobs = 6;
       J.maxlev = std::max(B.c_hi - B.c_lo + 1, B.f_hi - B.f_lo + 1);
-      launch_zfwd<R>(J, db, *B.pz, h->tx, 1.0 / db.ngz, st);
+      o.zf = J;
+    }
+  }
+  return nbl;
+}
+
+// The nonlinear term's plane work, one band at a time (one band without
+// variable resolution).  The flags select parts (the autotuner times them
+// separately); a substage runs all three.
+template <typename R>
+void enqueue_nonlinear(lh_handle* h, cudaStream_t st, bool zinv, bool xprod, bool zfwd) {
+  NlBand<R> bl[3];
+  const int nbl = nl_bands<R>(h, bl);
+  for (int b = 0; b < nbl; ++b) {
+    const NlBand<R>& B = bl[b];
+    if (zinv) {
+      launch_zinv<R>(B.zi, *B.d, *B.pz, h->tx, st);
+      mark(h, K_ZINV);
+    }
+    if (xprod) {
+      launch_xprod<R>(B.xp, *B.d, *B.ph, *B.pf, B.rtw, st);
+      mark(h, K_XPROD);
+    }
+    if (zfwd) {
+      launch_zfwd<R>(B.zf, *B.d, *B.pz, h->tx, 1.0 / B.d->ngz, st);
       mark(h, K_ZFWD);
     }
   }
@@ -415,63 +451,88 @@ float time_parts(lh_handle* h, bool z, bool x, cudaEvent_t e0, cudaEvent_t e1) {
   return best;
 }
 
+// RHS0 + nonlinear term + u + dt*du, divided by axz: the assembly of substage k.
+template <typename R>
+AsmArgs asm_args(const lh_handle* h, int k) {
+  AsmArgs a{};
+  a.u1 = h->u1; a.u2 = h->u2; a.u3 = h->u3; a.p = h->p;
+  a.n1 = h->n1; a.n2 = h->n2; a.n3 = h->n3;
+  a.r1 = h->r1; a.r2 = h->r2; a.r3 = h->r3;
+  {
+    const double2* pr[6] = {h->puu, h->puw, h->pww, h->pvv, h->puv, h->pvw};
+    for (int q = 0; q < 6; ++q) {
+      if (sizeof(R) == 4) a.p32[q] = reinterpret_cast<const float2*>(pr[q]);
+      else a.p64[q] = pr[q];
+    }
+  }
+  a.lytip = h->lytip;
+  a.tipu[0] = h->tipu[0]; a.tipu[1] = h->tipu[1]; a.tipv[0] = h->tipv[0]; a.tipv[1] = h->tipv[1];
+  a.sc = h->sc;
+  a.C1 = h->aRK[k] / h->Re; a.C2 = -h->cRK[k]; a.d = h->dRK[k]; a.g = h->gRK[k];
+  a.dt = h->dt; a.beta = h->bRK[k] * h->dt / h->Re; a.k = k;
+  return a;
+}
+
+// The canopy forcing of substage k: z-inverse of the processed planes, the x pass with the mask, z-forward
+// (false without canopy planes).
+template <typename R>
+bool ib_args(const lh_handle* h, int k, ZJobs<R>* zi, MaskArgs<R>* m, ZJobs<R>* zf) {
+  using T2 = cpx_t<R>;
+  if (h->nibu + h->nibv == 0) return false;
+  const size_t mp = h->d.mp;
+  T2* mib = (T2*)h->mixib;
+  ZJobs<R> J{};
+  J.j[0] = ZJob<R>{h->r1, nullptr, mib, h->ibu_lev, 0, h->nibu};
+  J.j[1] = ZJob<R>{h->r3, nullptr, mib + (size_t)h->nibu * mp, h->ibu_lev, 0, h->nibu};
+  J.j[2] = ZJob<R>{h->r2, nullptr, mib + (size_t)2 * h->nibu * mp, h->ibv_lev, 0, h->nibv};
+  J.j[3] = ZJob<R>{h->lytip, nullptr, (T2*)h->mixly, nullptr, 0, 6};
+  J.njobs = 4;
+  J.maxlev = std::max(std::max(h->nibu, h->nibv), 6);
+  *zi = J;
+  MaskArgs<R> a{};
+  a.mix = mib;
+  a.lymix = (const T2*)h->mixly;
+  a.mask[0] = h->ibu_mask; a.mask[1] = h->ibu_mask; a.mask[2] = h->ibv_mask;
+  a.tipslot[0] = h->ibu_tip; a.tipslot[1] = h->ibw_tip; a.tipslot[2] = h->ibv_tip;
+  a.nplanes[0] = h->nibu; a.nplanes[1] = h->nibu; a.nplanes[2] = h->nibv;
+  a.beta = h->bRK[k] * h->dt / h->Re;
+  *m = a;
+  ZJobs<R> F{};
+  F.j[0] = ZJob<R>{nullptr, h->r1, mib, h->ibu_lev, 0, h->nibu};
+  F.j[1] = ZJob<R>{nullptr, h->r3, mib + (size_t)h->nibu * mp, h->ibu_lev, 0, h->nibu};
+  F.j[2] = ZJob<R>{nullptr, h->r2, mib + (size_t)2 * h->nibu * mp, h->ibv_lev, 0, h->nibv};
+  F.njobs = 3;
+  F.maxlev = std::max(h->nibu, h->nibv);
+  *zf = F;
+  return true;
+}
+
+// solveP + v_corr of substage k (psolve's scalars)
+void psolve_scalars(const lh_handle* h, int k, double* dtirk, double* dtrk) {
+  const double dti = 1.0 / h->dt;
+  *dtirk = dti / (h->aRK[k] + h->bRK[k]);
+  *dtrk = h->dt * (h->aRK[k] + h->bRK[k]);
+}
+
 template <typename R>
 int enqueue_substage(lh_handle* h, int k, int upto) {
-  using T2 = cpx_t<R>;
   const Dims& d = h->d;
   cudaStream_t st = h->st;
-  const double beta = h->bRK[k] * h->dt / h->Re;
   enqueue_nonlinear<R>(h, st, true, true, true);
-  {
-    AsmArgs a{};
-    a.u1 = h->u1; a.u2 = h->u2; a.u3 = h->u3; a.p = h->p;
-    a.n1 = h->n1; a.n2 = h->n2; a.n3 = h->n3;
-    a.r1 = h->r1; a.r2 = h->r2; a.r3 = h->r3;
-    {
-      const double2* pr[6] = {h->puu, h->puw, h->pww, h->pvv, h->puv, h->pvw};
-      for (int q = 0; q < 6; ++q) {
-        if (sizeof(R) == 4) a.p32[q] = reinterpret_cast<const float2*>(pr[q]);
-        else a.p64[q] = pr[q];
-      }
-    }
-    a.lytip = h->lytip;
-    a.tipu[0] = h->tipu[0]; a.tipu[1] = h->tipu[1]; a.tipv[0] = h->tipv[0]; a.tipv[1] = h->tipv[1];
-    a.sc = h->sc;
-    a.C1 = h->aRK[k] / h->Re; a.C2 = -h->cRK[k]; a.d = h->dRK[k]; a.g = h->gRK[k];
-    a.dt = h->dt; a.beta = beta; a.k = k;
-    launch_assemble(a, d, h->t, st);
-    mark(h, K_ASSEMBLE);
-  }
+  launch_assemble(asm_args<R>(h, k), d, h->t, st);
+  mark(h, K_ASSEMBLE);
   if (upto <= 1) return LH_OK;
-  if (h->nibu + h->nibv > 0) {
-    const size_t mp = d.mp;
-    T2* mib = (T2*)h->mixib;
-    ZJobs<R> J{};
-    J.j[0] = ZJob<R>{h->r1, nullptr, mib, h->ibu_lev, 0, h->nibu};
-    J.j[1] = ZJob<R>{h->r3, nullptr, mib + (size_t)h->nibu * mp, h->ibu_lev, 0, h->nibu};
-    J.j[2] = ZJob<R>{h->r2, nullptr, mib + (size_t)2 * h->nibu * mp, h->ibv_lev, 0, h->nibv};
-    J.j[3] = ZJob<R>{h->lytip, nullptr, (T2*)h->mixly, nullptr, 0, 6};
-    J.njobs = 4;
-    J.maxlev = std::max(std::max(h->nibu, h->nibv), 6);
-    launch_zinv<R>(J, d, h->pz.plan, h->tx, st);
-    mark(h, K_IB_ZINV);
-    MaskArgs<R> m{};
-    m.mix = mib;
-    m.lymix = (const T2*)h->mixly;
-    m.mask[0] = h->ibu_mask; m.mask[1] = h->ibu_mask; m.mask[2] = h->ibv_mask;
-    m.tipslot[0] = h->ibu_tip; m.tipslot[1] = h->ibw_tip; m.tipslot[2] = h->ibv_tip;
-    m.nplanes[0] = h->nibu; m.nplanes[1] = h->nibu; m.nplanes[2] = h->nibv;
-    m.beta = beta;
-    launch_xmask<R>(m, d, h->ph.plan, h->rtw, st);
-    mark(h, K_IB_XMASK);
-    ZJobs<R> F{};
-    F.j[0] = ZJob<R>{nullptr, h->r1, mib, h->ibu_lev, 0, h->nibu};
-    F.j[1] = ZJob<R>{nullptr, h->r3, mib + (size_t)h->nibu * mp, h->ibu_lev, 0, h->nibu};
-    F.j[2] = ZJob<R>{nullptr, h->r2, mib + (size_t)2 * h->nibu * mp, h->ibv_lev, 0, h->nibv};
-    F.njobs = 3;
-    F.maxlev = std::max(h->nibu, h->nibv);
-    launch_zfwd<R>(F, d, h->pz.plan, h->tx, 1.0 / d.ngz, st);
-    mark(h, K_IB_ZFWD);
+  {
+    ZJobs<R> zi, zf;
+    MaskArgs<R> m;
+    if (ib_args<R>(h, k, &zi, &m, &zf)) {
+      launch_zinv<R>(zi, d, h->pz.plan, h->tx, st);
+      mark(h, K_IB_ZINV);
+      launch_xmask<R>(m, d, h->ph.plan, h->rtw, st);
+      mark(h, K_IB_XMASK);
+      launch_zfwd<R>(zf, d, h->pz.plan, h->tx, 1.0 / d.ngz, st);
+      mark(h, K_IB_ZFWD);
+    }
   }
   if (upto <= 2) return LH_OK;
   launch_vsolve(h->r1, h->r2, h->r3, h->u1, h->u2, h->u3, d, h->t, k, st);
@@ -482,9 +543,8 @@ int enqueue_substage(lh_handle* h, int k, int upto) {
     mark(h, K_FLOWRATE);
   }
   if (upto <= 4) return LH_OK;
-  const double dti = 1.0 / h->dt;
-  const double dtirk = dti / (h->aRK[k] + h->bRK[k]);
-  const double dtrk = h->dt * (h->aRK[k] + h->bRK[k]);
+  double dtirk, dtrk;
+  psolve_scalars(h, k, &dtirk, &dtrk);
   launch_psolve(h->u1, h->u2, h->u3, h->p, h->psi, d, h->t, dtirk, dtrk, h->gw[0][0], h->gw[2][1], h->sc, st);
   mark(h, K_PSOLVE);
   return LH_OK;
@@ -1128,6 +1188,9 @@ struct lh_ensemble {
   std::vector<cudaEvent_t> ev;  // fork event, then one join event per member
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   double last_ms = 0;
+  int mode = LH_ENS_STREAMS;     // requested mode (streams: the faster at the sizes measured)
+  int used = LH_ENS_STREAMS;     // mode of the captured graph
+  int launches = 0;              // kernels per step in the captured graph
   std::string err;
 };
 
@@ -1144,6 +1207,223 @@ int ens_fail(lh_ensemble* e, int code, const char* msg, cudaError_t ce = cudaSuc
   if (ce != cudaSuccess) { e->err += ": "; e->err += cudaGetErrorString(ce); }
   return code;
 }
+
+extern "C++" {
+// Batched mode: one launch per kernel kind and slot of the substage (the bands' z-inverse, product pass and
+// z-forward, assembly, canopy forcing, Thomas sweeps, flow rate, pressure solve), each covering every member
+// that has that launch; the members' arguments are descriptors in one device buffer.
+struct Slot {
+  int kind;                          // K_*
+  size_t smem;
+  std::vector<unsigned char> param;  // the Batch<D> kernel parameter
+};
+
+// Appends the slots of one kernel kind from the members' descriptors (members without the launch pass none):
+// one launch per distinct dynamic shared-memory size (a launch reserves one size for all its blocks, so members
+// of a larger grid class would lower the occupancy of the others), kMaxBatch members per launch.
+template <typename D>
+void add_slot(std::vector<Slot>& slots, int kind, const std::vector<D>& ds, const std::vector<int>& blocks,
+              const std::vector<size_t>& smem) {
+  std::vector<size_t> sizes(smem);
+  std::sort(sizes.begin(), sizes.end());
+  sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
+  for (size_t sz : sizes) {
+    std::vector<size_t> mine;
+    for (size_t m = 0; m < ds.size(); ++m)
+      if (smem[m] == sz) mine.push_back(m);
+    for (size_t lo = 0; lo < mine.size(); lo += kMaxBatch) {
+      const size_t n = std::min(mine.size() - lo, (size_t)kMaxBatch);
+      Slot sl{};
+      sl.kind = kind;
+      sl.smem = sz;
+      sl.param.assign(sizeof(Batch<D>), 0);
+      Batch<D>* b = reinterpret_cast<Batch<D>*>(sl.param.data());
+      b->n = (int)n;
+      int tot = 0;
+      for (size_t q = 0; q < n; ++q) {
+        const size_t m = mine[lo + q];
+        b->start[q] = tot;
+        tot += blocks[m];
+        b->desc[q] = ds[m];
+      }
+      b->start[n] = tot;
+      slots.push_back(std::move(sl));
+    }
+  }
+}
+
+template <typename R>
+void build_batched(const std::vector<lh_handle*>& hs, std::vector<Slot>& slots) {
+  const size_t nm = hs.size();
+  for (int k = 0; k < 3; ++k) {
+    std::vector<NlBand<R>> nl(3 * nm);
+    std::vector<int> nb(nm);
+    for (size_t m = 0; m < nm; ++m) nb[m] = nl_bands<R>(hs[m], &nl[3 * m]);
+    for (int b = 0; b < 3; ++b) {
+      for (int part = 0; part < 3; ++part) {  // z-inverse, product pass, z-forward of band b
+        std::vector<ZDesc<R>> zd;
+        std::vector<XDesc<R>> xd;
+        std::vector<int> blocks;
+        std::vector<size_t> smem;
+        for (size_t m = 0; m < nm; ++m) {
+          if (nb[m] <= b) continue;
+          const lh_handle* h = hs[m];
+          const NlBand<R>& B = nl[3 * m + b];
+          dim3 g;
+          size_t sm;
+          if (part == 1) {
+            xprod_shape<R>(B.xp, *B.d, &g, &sm);
+            if (g.x == 0) continue;
+            XDesc<R> D{};
+            D.a = B.xp; D.d = *B.d; D.ph = *B.ph; D.pf = *B.pf; D.rtw = B.rtw; D.gx = g.x; D.gy = g.y;
+            xd.push_back(D);
+          } else {
+            const ZJobs<R>& J = part == 0 ? B.zi : B.zf;
+            zpass_shape<R>(J, *B.d, h->tx, &g, &sm);
+            if (g.x == 0) continue;
+            ZDesc<R> D{};
+            D.jobs = J; D.d = *B.d; D.p = *B.pz; D.scale = 1.0 / B.d->ngz; D.tx = h->tx;
+            D.gx = g.x; D.gy = g.y; D.gz = g.z;
+            zd.push_back(D);
+          }
+          blocks.push_back((int)(g.x * g.y * g.z));
+          smem.push_back(sm);
+        }
+        if (part == 1) add_slot(slots, K_XPROD, xd, blocks, smem);
+        else add_slot(slots, part == 0 ? K_ZINV : K_ZFWD, zd, blocks, smem);
+      }
+    }
+    {
+      std::vector<ADesc> ad;
+      std::vector<int> blocks;
+      for (lh_handle* h : hs) {
+        ADesc D{};
+        D.a = asm_args<R>(h, k); D.d = h->d; D.t = h->t;
+        D.gx = (h->d.np + 255) / 256; D.gy = h->d.nyu;
+        ad.push_back(D);
+        blocks.push_back(D.gx * D.gy);
+      }
+      add_slot(slots, K_ASSEMBLE, ad, blocks, std::vector<size_t>(ad.size(), 0));
+    }
+    {
+      std::vector<ZDesc<R>> zi, zf;
+      std::vector<MDesc<R>> md;
+      std::vector<int> bi, bm, bf;
+      std::vector<size_t> si, sm_, sf;
+      for (lh_handle* h : hs) {
+        ZJobs<R> a, c;
+        MaskArgs<R> mk;
+        if (!ib_args<R>(h, k, &a, &mk, &c)) continue;
+        dim3 g;
+        size_t sm;
+        zpass_shape<R>(a, h->d, h->tx, &g, &sm);
+        ZDesc<R> Di{};
+        Di.jobs = a; Di.d = h->d; Di.p = h->pz.plan; Di.scale = 1.0; Di.tx = h->tx; Di.gx = g.x; Di.gy = g.y; Di.gz = g.z;
+        zi.push_back(Di); bi.push_back((int)(g.x * g.y * g.z)); si.push_back(sm);
+        xmask_shape<R>(mk, h->d, &g, &sm);
+        MDesc<R> Dm{};
+        Dm.a = mk; Dm.d = h->d; Dm.ph = h->ph.plan; Dm.rtw = h->rtw; Dm.gx = g.x; Dm.gy = g.y;
+        md.push_back(Dm); bm.push_back((int)(g.x * g.y)); sm_.push_back(sm);
+        zpass_shape<R>(c, h->d, h->tx, &g, &sm);
+        ZDesc<R> Df{};
+        Df.jobs = c; Df.d = h->d; Df.p = h->pz.plan; Df.scale = 1.0 / h->d.ngz; Df.tx = h->tx;
+        Df.gx = g.x; Df.gy = g.y; Df.gz = g.z;
+        zf.push_back(Df); bf.push_back((int)(g.x * g.y * g.z)); sf.push_back(sm);
+      }
+      add_slot(slots, K_IB_ZINV, zi, bi, si);
+      add_slot(slots, K_IB_XMASK, md, bm, sm_);
+      add_slot(slots, K_IB_ZFWD, zf, bf, sf);
+    }
+    {
+      std::vector<VDesc> vd;
+      std::vector<FDesc> fd;
+      std::vector<PDesc> pd;
+      std::vector<int> bv, bfl, bp;
+      for (lh_handle* h : hs) {
+        VDesc V{};
+        V.r1 = h->r1; V.r2 = h->r2; V.r3 = h->r3; V.u1 = h->u1; V.u2 = h->u2; V.u3 = h->u3;
+        V.d = h->d; V.t = h->t; V.k = k; V.gx = (h->d.np + 127) / 128; V.gy = 3;
+        vd.push_back(V); bv.push_back(V.gx * V.gy);
+        if (h->prm.flag_ctpress == 0) {
+          FDesc F{};
+          F.u1 = h->u1; F.sc = h->sc; F.d = h->d; F.t = h->t; F.k = k; F.Qx1 = h->Qx1[k];
+          fd.push_back(F); bfl.push_back(1);
+        }
+        PDesc P{};
+        P.u1 = h->u1; P.u2 = h->u2; P.u3 = h->u3; P.p = h->p; P.psi = h->psi; P.d = h->d; P.t = h->t;
+        psolve_scalars(h, k, &P.dtirk, &P.dtrk);
+        P.gwb = h->gw[0][0]; P.gwt = h->gw[2][1]; P.sc = h->sc; P.gx = (h->d.np + 127) / 128;
+        pd.push_back(P); bp.push_back(P.gx);
+      }
+      add_slot(slots, K_VSOLVE, vd, bv, std::vector<size_t>(vd.size(), 0));
+      add_slot(slots, K_FLOWRATE, fd, bfl, std::vector<size_t>(fd.size(), 0));
+      add_slot(slots, K_PSOLVE, pd, bp, std::vector<size_t>(pd.size(), 0));
+    }
+  }
+}
+
+template <typename R>
+void launch_slot(const Slot& sl, cudaStream_t st) {
+  const void* p = sl.param.data();
+  switch (sl.kind) {
+    case K_ZINV: case K_IB_ZINV: launch_zinv_batch<R>(*(const Batch<ZDesc<R>>*)p, sl.smem, st); break;
+    case K_ZFWD: case K_IB_ZFWD: launch_zfwd_batch<R>(*(const Batch<ZDesc<R>>*)p, sl.smem, st); break;
+    case K_XPROD: launch_xprod_batch<R>(*(const Batch<XDesc<R>>*)p, sl.smem, st); break;
+    case K_IB_XMASK: launch_xmask_batch<R>(*(const Batch<MDesc<R>>*)p, sl.smem, st); break;
+    case K_ASSEMBLE: launch_assemble_batch(*(const Batch<ADesc>*)p, sizeof(R) == 4, st); break;
+    case K_VSOLVE: launch_vsolve_batch(*(const Batch<VDesc>*)p, st); break;
+    case K_FLOWRATE: launch_flowrate_batch(*(const Batch<FDesc>*)p, st); break;
+    default: launch_psolve_batch(*(const Batch<PDesc>*)p, st); break;
+  }
+}
+
+// Capture of one RK3 step of every member in batched launches (the caller checked that all members share a
+// precision).  Members with the same grid form a class; each class's batched launches go to a stream of their own
+// (the class's first member's), forked from and joined to the origin, so that the classes' kernels overlap as
+// the members' do in the streams mode.  The launch arguments live in the graph's kernel nodes.
+template <typename R>
+int capture_batched(lh_ensemble* e, cudaGraph_t* g) {
+  std::vector<std::vector<lh_handle*>> classes;
+  for (lh_handle* h : e->hs) {
+    bool put = false;
+    for (auto& c : classes) {
+      const Dims& a = c[0]->d;
+      const Dims& b = h->d;
+      if (a.ngx == b.ngx && a.ngz == b.ngz && a.nyu == b.nyu && a.banded == b.banded && a.ngx2 == b.ngx2 &&
+          a.ngz2 == b.ngz2) {
+        c.push_back(h);
+        put = true;
+        break;
+      }
+    }
+    if (!put) classes.push_back({h});
+  }
+  std::vector<std::vector<Slot>> slots(classes.size());
+  for (size_t c = 0; c < classes.size(); ++c) build_batched<R>(classes[c], slots[c]);
+  for (lh_handle* h : e->hs) {  // the members' own streams may still hold work on their fields
+    const cudaError_t ce = cudaStreamSynchronize(h->st);
+    if (ce != cudaSuccess) return ens_fail(e, LH_ECUDA, "member stream", ce);
+  }
+  cudaError_t ce = cudaStreamBeginCapture(e->origin, cudaStreamCaptureModeThreadLocal);
+  if (ce != cudaSuccess) return ens_fail(e, LH_ECUDA, "capture", ce);
+  cudaEventRecord(e->ev[0], e->origin);
+  int launches = 0;
+  for (size_t c = 0; c < classes.size(); ++c) {
+    cudaStream_t st = classes[c][0]->st;
+    cudaStreamWaitEvent(st, e->ev[0], 0);
+    for (const Slot& sl : slots[c]) launch_slot<R>(sl, st);
+    cudaEventRecord(e->ev[c + 1], st);
+    cudaStreamWaitEvent(e->origin, e->ev[c + 1], 0);
+    launches += (int)slots[c].size();
+  }
+  const cudaError_t le = cudaGetLastError();
+  ce = cudaStreamEndCapture(e->origin, g);
+  if (le != cudaSuccess) { if (*g) cudaGraphDestroy(*g); return ens_fail(e, LH_ECUDA, "batched launch", le); }
+  if (ce != cudaSuccess) return ens_fail(e, LH_ECUDA, "capture", ce);
+  e->launches = launches;
+  return LH_OK;
+}
+}  // extern "C++"
 }  // namespace
 
 int lh_ensemble_create(lh_handle* const* hs, int32_t n, lh_ensemble** out) {
@@ -1187,6 +1467,25 @@ void lh_ensemble_free(lh_ensemble* e) {
 
 const char* lh_ensemble_last_error(const lh_ensemble* e) { return e ? e->err.c_str() : ""; }
 
+int lh_ensemble_set_mode(lh_ensemble* e, int32_t mode) {
+  if (!e) return LH_EINVAL;
+  if (mode != LH_ENS_BATCHED && mode != LH_ENS_STREAMS) return ens_fail(e, LH_EINVAL, "unknown ensemble mode");
+  if (mode != e->mode && e->graph) {
+    cudaSetDevice(e->device);
+    cudaGraphExecDestroy(e->graph);
+    e->graph = nullptr;
+  }
+  e->mode = mode;
+  return LH_OK;
+}
+
+int lh_ensemble_info(const lh_ensemble* e, int32_t* mode_used, int32_t* launches_per_step) {
+  if (!e) return LH_EINVAL;
+  if (mode_used) *mode_used = e->used;
+  if (launches_per_step) *launches_per_step = e->launches;
+  return LH_OK;
+}
+
 int lh_ensemble_step(lh_ensemble* e, int32_t nsteps, double* ms) {
   if (!e) return LH_EINVAL;
   if (nsteps < 0) return ens_fail(e, LH_EINVAL, "nsteps < 0");
@@ -1202,23 +1501,35 @@ int lh_ensemble_step(lh_ensemble* e, int32_t nsteps, double* ms) {
   }
   if (!e->graph) {
     cudaGraph_t g = nullptr;
-    cudaError_t ce = cudaStreamBeginCapture(e->origin, cudaStreamCaptureModeThreadLocal);
-    if (ce != cudaSuccess) return ens_fail(e, LH_ECUDA, "capture", ce);
-    int rc = LH_OK;
-    cudaEventRecord(e->ev[0], e->origin);
-    for (size_t i = 0; i < e->hs.size() && rc == LH_OK; ++i) {
-      lh_handle* h = e->hs[i];
-      cudaStreamWaitEvent(h->st, e->ev[0], 0);
-      for (int k = 0; k < 3 && rc == LH_OK; ++k) rc = substage(h, k, 5);
-      cudaEventRecord(e->ev[i + 1], h->st);
-      cudaStreamWaitEvent(e->origin, e->ev[i + 1], 0);
+    cudaError_t ce = cudaSuccess;
+    bool same = true;
+    for (lh_handle* h : e->hs) same = same && h->precision == e->hs[0]->precision;
+    if (e->mode == LH_ENS_BATCHED && same) {
+      const int rc = e->hs[0]->precision == LH_PREC_MIXED ? capture_batched<float>(e, &g) : capture_batched<double>(e, &g);
+      if (rc) return rc;
+      e->used = LH_ENS_BATCHED;
+    } else {
+      ce = cudaStreamBeginCapture(e->origin, cudaStreamCaptureModeThreadLocal);
+      if (ce != cudaSuccess) return ens_fail(e, LH_ECUDA, "capture", ce);
+      int rc = LH_OK;
+      cudaEventRecord(e->ev[0], e->origin);
+      for (size_t i = 0; i < e->hs.size() && rc == LH_OK; ++i) {
+        lh_handle* h = e->hs[i];
+        cudaStreamWaitEvent(h->st, e->ev[0], 0);
+        for (int k = 0; k < 3 && rc == LH_OK; ++k) rc = substage(h, k, 5);
+        cudaEventRecord(e->ev[i + 1], h->st);
+        cudaStreamWaitEvent(e->origin, e->ev[i + 1], 0);
+      }
+      ce = cudaStreamEndCapture(e->origin, &g);
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return ens_fail(e, rc, "capture of a member failed");
+      }
+      if (ce != cudaSuccess) return ens_fail(e, LH_ECUDA, "capture", ce);
+      e->used = LH_ENS_STREAMS;
+      e->launches = 0;
+      for (lh_handle* h : e->hs) e->launches += h->launches_per_step;
     }
-    ce = cudaStreamEndCapture(e->origin, &g);
-    if (rc) {
-      if (g) cudaGraphDestroy(g);
-      return ens_fail(e, rc, "capture of a member failed");
-    }
-    if (ce != cudaSuccess) return ens_fail(e, LH_ECUDA, "capture", ce);
     ce = cudaGraphInstantiate(&e->graph, g, 0);
     cudaGraphDestroy(g);
     if (ce != cudaSuccess) { e->graph = nullptr; return ens_fail(e, LH_ECUDA, "instantiate", ce); }

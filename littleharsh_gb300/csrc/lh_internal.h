@@ -116,6 +116,7 @@ struct ZJob {
   const int* levels;
   int lev0, nlev;
   int out32;                // z-forward: write FP32 spectra (cpx_t<R>) to spec_out instead of FP64
+  int nomean;               // z-inverse: leave the (0,0) mode out (the mixed form carries the mean profile apart)
 };
 
 constexpr int kMaxJobs = 12;
@@ -147,6 +148,14 @@ struct ProdArgs {
   int split;            // 1: the face pair is transformed after the centre pairs, through two buffer vectors
   // levels this launch forms products on (a band's planes): centres c_lo..c_hi, faces f_lo..f_hi
   int c_lo, c_hi, f_lo, f_hi;
+  // mixed form: mu, mw hold the fluctuations u' = u - U(y), w' = w - W(y) (the z-inverse left the (0,0) modes
+  // out) and the products are formed as u'(2U + u'), u'(W + w') + U w', w'(2W + w'), (U_f + u'_f) v,
+  // (W_f + w'_f) v with the level means U, W read from the (0,0) modes of us, ws (nps apart): the FP32 values
+  // never hold U^2 beside products ten to a hundred times smaller.  The left-out U^2, UW reach only the (0,0)
+  // modes of uu, uw, ww, of which the nonlinear term takes no derivative.
+  int mean_split;
+  const double2 *us, *ws;
+  int nps;
 };
 template <typename R>
 void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const FftPlan& pf, const double2* rtw,
@@ -215,6 +224,100 @@ struct CondArgs {
 void launch_stage_itp(const double2* u2, const double2* u3, double2* vc, double2* wf, double2* om, const Dims& d,
                       const Tables& t, cudaStream_t st);
 void launch_xcond(const CondArgs& a, const Dims& d, const FftPlan& ph, const double2* rtw, cudaStream_t st);
+// ---------------------------------------------------------------------------
+// Batched launches: one launch of a kernel kind covers the work of several
+// independent solvers (an ensemble).  The members' arguments travel as one
+// kernel parameter (Batch<D>, under the 32 KB parameter limit), read from the
+// constant bank like a single launch's; member m owns the blocks start[m] ..
+// start[m+1]-1 of the launch's one-dimensional grid, laid out as its own
+// gx x gy x gz grid would be.  The arithmetic of a block is that of the
+// single-solver launch, so the results are bit for bit the same.
+// ---------------------------------------------------------------------------
+constexpr int kMaxBatch = 32;   // members per batched launch (larger ensembles take several)
+template <typename R>
+struct ZDesc {                  // z-inverse or z-forward
+  ZJobs<R> jobs;
+  Dims d;
+  FftPlan p;
+  double scale;
+  int tx, gx, gy, gz;
+};
+template <typename R>
+struct XDesc {                  // x pass with the products
+  ProdArgs<R> a;
+  Dims d;
+  FftPlan ph, pf;
+  const double2* rtw;
+  int gx, gy;
+};
+template <typename R>
+struct MDesc {                  // canopy forcing x pass
+  MaskArgs<R> a;
+  Dims d;
+  FftPlan ph;
+  const double2* rtw;
+  int gx, gy;
+};
+struct ADesc {                  // right-hand-side assembly
+  AsmArgs a;
+  Dims d;
+  Tables t;
+  int gx, gy;
+};
+struct VDesc {                  // velocity Thomas sweeps
+  double2 *r1, *r2, *r3, *u1, *u2, *u3;
+  Dims d;
+  Tables t;
+  int k, gx, gy;
+};
+struct FDesc {                  // flow-rate correction (one block)
+  double2* u1;
+  DevScalars* sc;
+  Dims d;
+  Tables t;
+  int k;
+  double Qx1;
+};
+struct PDesc {                  // pressure solve and correction
+  double2 *u1, *u2, *u3, *p, *psi;
+  Dims d;
+  Tables t;
+  double dtirk, dtrk, gwb, gwt;
+  DevScalars* sc;
+  int gx;
+};
+template <typename D>
+struct Batch {
+  int n;                      // members in this launch
+  int start[kMaxBatch + 1];   // first block of each member, start[n] = total blocks
+  D desc[kMaxBatch];
+};
+static_assert(sizeof(Batch<ZDesc<double>>) < 32700 && sizeof(Batch<XDesc<double>>) < 32700 &&
+                  sizeof(Batch<ADesc>) < 32700 && sizeof(Batch<MDesc<double>>) < 32700,
+              "a batch must fit the kernel parameter limit");
+// Launchers of the batched kernels (start[] filled from the members' gx*gy*gz; smem: the largest dynamic shared
+// memory any member needs).
+template <typename R>
+void launch_zinv_batch(const Batch<ZDesc<R>>& b, size_t smem, cudaStream_t st);
+template <typename R>
+void launch_zfwd_batch(const Batch<ZDesc<R>>& b, size_t smem, cudaStream_t st);
+template <typename R>
+void launch_xprod_batch(const Batch<XDesc<R>>& b, size_t smem, cudaStream_t st);
+template <typename R>
+void launch_xmask_batch(const Batch<MDesc<R>>& b, size_t smem, cudaStream_t st);
+void launch_assemble_batch(const Batch<ADesc>& b, bool fp32_products, cudaStream_t st);
+void launch_vsolve_batch(const Batch<VDesc>& b, cudaStream_t st);
+void launch_flowrate_batch(const Batch<FDesc>& b, cudaStream_t st);
+void launch_psolve_batch(const Batch<PDesc>& b, cudaStream_t st);
+// Grid and dynamic shared memory of the single launches (what the batched ones reproduce per member; a zero
+// grid means no launch).
+template <typename R>
+void zpass_shape(const ZJobs<R>& jobs, const Dims& d, int tx, dim3* grid, size_t* smem);
+template <typename R>
+void xprod_shape(const ProdArgs<R>& a, const Dims& d, dim3* grid, size_t* smem);
+template <typename R>
+void xmask_shape(const MaskArgs<R>& a, const Dims& d, dim3* grid, size_t* smem);
+
 cudaError_t configure_kernels();
 // Measured FP64 FMA throughput of the current device in TFLOP/s (FMA = 2 flops), best of three timed
 // launches of a probe kernel; -1 on a CUDA error.  nsm_out (may be NULL) receives the SM count.

@@ -35,16 +35,17 @@ namespace lh {
 // ---------------------------------------------------------------------------
 
 template <typename R>
-__global__ void __launch_bounds__(256) k_zinv(ZJobs<R> jobs, Dims d, FftPlan pz, int tx) {
+__device__ __forceinline__ void zinv_body(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, int bx,
+                                          int by, int bz) {
   using T2 = cpx_t<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   T2* sm = reinterpret_cast<T2*>(smraw);  // [ngz][tx]
-  const int job = blockIdx.z;
+  const int job = bz;
   const ZJob<R> J = jobs.j[job];
-  const int y = blockIdx.y;
+  const int y = by;
   if (y >= J.nlev) return;
   const int lev = J.levels ? J.levels[y] : J.lev0 + y;
-  const int i0 = blockIdx.x * tx;
+  const int i0 = bx * tx;
   const int nb = min(tx, d.nkx - i0);
   const double2* __restrict__ src = J.spec_in + (size_t)lev * d.np;
   const int h = d.nz / 2, gap = d.ngz - d.nz;
@@ -54,7 +55,7 @@ __global__ void __launch_bounds__(256) k_zinv(ZJobs<R> jobs, Dims d, FftPlan pz,
     const int kk = e / tx, c = e - kk * tx;
     const int slot = kk < h ? kk : kk + gap;
     T2 v = T2{0, 0};
-    if (c < nb) {
+    if (c < nb && !(J.nomean && kk == 0 && i0 + c == 0)) {
       const int ks = kk < h ? kk : kk - d.nz + d.snz;  // row of the stored mode set
       const double2 s = src[(size_t)ks * d.spitch + i0 + c];
       v = T2{(R)s.x, (R)s.y};
@@ -71,16 +72,23 @@ __global__ void __launch_bounds__(256) k_zinv(ZJobs<R> jobs, Dims d, FftPlan pz,
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256) k_zfwd(ZJobs<R> jobs, Dims d, FftPlan pz, int tx, double scale) {
+__global__ void __launch_bounds__(256) k_zinv(const __grid_constant__ ZJobs<R> jobs, const __grid_constant__ Dims d,
+                                              const __grid_constant__ FftPlan pz, int tx) {
+  zinv_body<R>(jobs, d, pz, tx, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <typename R>
+__device__ __forceinline__ void zfwd_body(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, double scale,
+                                          int bx, int by, int bz) {
   using T2 = cpx_t<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   T2* sm = reinterpret_cast<T2*>(smraw);  // [ngz][tx]
-  const int job = blockIdx.z;
+  const int job = bz;
   const ZJob<R> J = jobs.j[job];
-  const int y = blockIdx.y;
+  const int y = by;
   if (y >= J.nlev) return;
   const int lev = J.levels ? J.levels[y] : J.lev0 + y;
-  const int i0 = blockIdx.x * tx;
+  const int i0 = bx * tx;
   const int nb = min(tx, d.nkx - i0);
   const T2* __restrict__ src = J.mix + (size_t)y * d.mp;
   for (int e = threadIdx.x; e < d.ngz * tx; e += blockDim.x) {
@@ -121,18 +129,32 @@ __global__ void __launch_bounds__(256) k_zfwd(ZJobs<R> jobs, Dims d, FftPlan pz,
 }
 
 template <typename R>
+__global__ void __launch_bounds__(256) k_zfwd(const __grid_constant__ ZJobs<R> jobs, const __grid_constant__ Dims d,
+                                              const __grid_constant__ FftPlan pz, int tx, double scale) {
+  zfwd_body<R>(jobs, d, pz, tx, scale, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <typename R>
+void zpass_shape(const ZJobs<R>& jobs, const Dims& d, int tx, dim3* grid, size_t* smem) {
+  *grid = (jobs.njobs == 0 || jobs.maxlev == 0) ? dim3(0, 0, 0) : dim3((d.nkx + tx - 1) / tx, jobs.maxlev, jobs.njobs);
+  *smem = sizeof(cpx_t<R>) * (size_t)d.ngz * tx;
+}
+
+template <typename R>
 void launch_zinv(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, cudaStream_t st) {
-  if (jobs.njobs == 0 || jobs.maxlev == 0) return;
-  dim3 grid((d.nkx + tx - 1) / tx, jobs.maxlev, jobs.njobs);
-  size_t sm = sizeof(cpx_t<R>) * (size_t)d.ngz * tx;
+  dim3 grid;
+  size_t sm;
+  zpass_shape(jobs, d, tx, &grid, &sm);
+  if (grid.x == 0) return;
   k_zinv<R><<<grid, 256, sm, st>>>(jobs, d, pz, tx);
 }
 
 template <typename R>
 void launch_zfwd(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, double scale, cudaStream_t st) {
-  if (jobs.njobs == 0 || jobs.maxlev == 0) return;
-  dim3 grid((d.nkx + tx - 1) / tx, jobs.maxlev, jobs.njobs);
-  size_t sm = sizeof(cpx_t<R>) * (size_t)d.ngz * tx;
+  dim3 grid;
+  size_t sm;
+  zpass_shape(jobs, d, tx, &grid, &sm);
+  if (grid.x == 0) return;
   k_zfwd<R><<<grid, 256, sm, st>>>(jobs, d, pz, tx, scale);
 }
 
@@ -254,8 +276,8 @@ __device__ void x_forward_pairs(int np2, cpx_t<R>* F, cpx_t<R>* const* rows, con
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph, FftPlan pf,
-                                               const double2* __restrict__ rtw) {
+__device__ __forceinline__ void xprod_body(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const FftPlan& pf,
+                                           const double2* __restrict__ rtw, int bx, int by) {
   using T2 = cpx_t<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ngx = d.ngx, h = ngx / 2, hp = h + 1;
@@ -269,10 +291,10 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
   R* wc = rowsm + 4 * ngx;
   R* vc = rowsm + 5 * ngx;
   __shared__ double cflred[8];
-  const int kz = blockIdx.x;
+  const int kz = bx;
   // step jj forms the centre-jj products (c_lo <= jj <= c_hi) and the face-(jj-1) ones (f_lo <= jj-1 <= f_hi)
   const int L0 = min(a.c_lo, a.f_lo + 1), L1 = max(a.c_hi, a.f_hi + 1);
-  const int c0 = L0 + blockIdx.y * a.chunk;
+  const int c0 = L0 + by * a.chunk;
   const int c1 = min(c0 + a.chunk - 1, L1);
   if (c0 > c1) return;
   const size_t rowoff = (size_t)kz * d.nkx;
@@ -308,18 +330,35 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
     // with a.split and both kinds, the face pair goes through the buffer after the centre pairs' transform
     const bool later = a.split && cprod && fprod;
     const int fslot = (cprod && !later) ? 2 : 0;
+    // mixed form: the level means at centre jj and face jj-1 (the FP64 form transforms u and w whole)
+    R Uc = (R)0, Wc = (R)0, Uf = (R)0, Wf = (R)0;
+    if constexpr (sizeof(R) == 4) {
+      if (a.mean_split) {
+        const R Um = (R)a.us[(size_t)(jj - 1) * a.nps].x, Wm = (R)a.ws[(size_t)(jj - 1) * a.nps].x;
+        Uc = (R)a.us[(size_t)jj * a.nps].x;
+        Wc = (R)a.ws[(size_t)jj * a.nps].x;
+        Uf = Um + wfj * (Uc - Um);
+        Wf = Wm + wfj * (Wc - Wm);
+      }
+    }
     auto face_pair = [&](int x, R u, R w, int px) {
       const R uf = up[x] + wfj * (u - up[x]);
       const R wf = wp[x] + wfj * (w - wp[x]);
-      F[sxi<R>(fslot * ngx + px)] = T2{uf * vp[x], wf * vp[x]};
+      if constexpr (sizeof(R) == 4) F[sxi<R>(fslot * ngx + px)] = T2{(Uf + uf) * vp[x], (Wf + wf) * vp[x]};
+      else F[sxi<R>(fslot * ngx + px)] = T2{uf * vp[x], wf * vp[x]};
     };
     for (int x = threadIdx.x; x < ngx; x += blockDim.x) {
       const R u = uc[x], w = wc[x];
       const int px = pf.perm[x];
       if (cprod) {
         const R v = vp[x] + wcj * (vc[x] - vp[x]);
-        F[sxi<R>(px)] = T2{u * u, u * w};
-        F[sxi<R>(ngx + px)] = T2{w * w, v * v};
+        if constexpr (sizeof(R) == 4) {
+          F[sxi<R>(px)] = T2{u * ((Uc + Uc) + u), u * (Wc + w) + Uc * w};
+          F[sxi<R>(ngx + px)] = T2{w * ((Wc + Wc) + w), v * v};
+        } else {
+          F[sxi<R>(px)] = T2{u * u, u * w};
+          F[sxi<R>(ngx + px)] = T2{w * w, v * v};
+        }
         if (a.want_cfl) {
           const double cv = fabs((double)u) * a.dxi + fabs((double)v) * dyi + fabs((double)w) * a.dzi;
           cmax = fmax(cmax, cv);
@@ -368,30 +407,45 @@ __global__ void __launch_bounds__(256) k_xprod(ProdArgs<R> a, Dims d, FftPlan ph
 }
 
 template <typename R>
-void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const FftPlan& pf, const double2* rtw,
-                  cudaStream_t st) {
+__global__ void __launch_bounds__(256) k_xprod(const __grid_constant__ ProdArgs<R> a, const __grid_constant__ Dims d,
+                                               const __grid_constant__ FftPlan ph, const __grid_constant__ FftPlan pf,
+                                               const double2* __restrict__ rtw) {
+  xprod_body<R>(a, d, ph, pf, rtw, blockIdx.x, blockIdx.y);
+}
+
+template <typename R>
+void xprod_shape(const ProdArgs<R>& a, const Dims& d, dim3* grid, size_t* smem) {
   const int L0 = std::min(a.c_lo, a.f_lo + 1), L1 = std::max(a.c_hi, a.f_hi + 1);
   const int nlev = L1 - L0 + 1;
-  if (nlev <= 0) return;
-  dim3 grid(d.ngz, (nlev + a.chunk - 1) / a.chunk);
-  size_t sm = sizeof(cpx_t<R>) * sx_elems<R>((a.split ? 2 : 3) * (size_t)d.ngx) + sizeof(R) * 6 * (size_t)d.ngx;
+  *grid = nlev <= 0 ? dim3(0, 0, 0) : dim3(d.ngz, (nlev + a.chunk - 1) / a.chunk);
+  *smem = sizeof(cpx_t<R>) * sx_elems<R>((a.split ? 2 : 3) * (size_t)d.ngx) + sizeof(R) * 6 * (size_t)d.ngx;
+}
+
+template <typename R>
+void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const FftPlan& pf, const double2* rtw,
+                  cudaStream_t st) {
+  dim3 grid;
+  size_t sm;
+  xprod_shape(a, d, &grid, &sm);
+  if (grid.x == 0) return;
   k_xprod<R><<<grid, 256, sm, st>>>(a, d, ph, pf, rtw);
 }
 
 // Canopy forcing on one mixed row of one processed plane: x-inverse, solid
 // points set to 0 (or -beta*Luy on the tip planes), x-forward.
 template <typename R>
-__global__ void __launch_bounds__(128) k_xmask(MaskArgs<R> a, Dims d, FftPlan ph, const double2* __restrict__ rtw) {
+__device__ __forceinline__ void xmask_body(const MaskArgs<R>& a, const Dims& d, const FftPlan& ph,
+                                           const double2* __restrict__ rtw, int bx, int by) {
   using T2 = cpx_t<R>;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int ngx = d.ngx, h = ngx / 2, hp = h + 1;
   T2* F = reinterpret_cast<T2*>(smraw);
   R* rr = reinterpret_cast<R*>(F + sx_elems<R>(2 * (size_t)hp));
   R* ll = rr + ngx;
-  const int kz = blockIdx.x;
-  int pl = blockIdx.y, f = 0;
+  const int kz = bx;
+  int pl = by, f = 0;
   while (f < 2 && pl >= a.nplanes[f]) { pl -= a.nplanes[f]; ++f; }
-  size_t plane = (size_t)blockIdx.y;
+  size_t plane = (size_t)by;
   T2* row = a.mix + plane * d.mp + (size_t)kz * d.nkx;
   const int tip = a.tipslot[f][pl];
   const uint8_t* msk = a.mask[f] + ((size_t)pl * d.ngz + kz) * ngx;
@@ -425,12 +479,25 @@ __global__ void __launch_bounds__(128) k_xmask(MaskArgs<R> a, Dims d, FftPlan ph
 }
 
 template <typename R>
-void launch_xmask(const MaskArgs<R>& a, const Dims& d, const FftPlan& ph, const double2* rtw, cudaStream_t st) {
+__global__ void __launch_bounds__(128) k_xmask(const __grid_constant__ MaskArgs<R> a, const __grid_constant__ Dims d,
+                                               const __grid_constant__ FftPlan ph, const double2* __restrict__ rtw) {
+  xmask_body<R>(a, d, ph, rtw, blockIdx.x, blockIdx.y);
+}
+
+template <typename R>
+void xmask_shape(const MaskArgs<R>& a, const Dims& d, dim3* grid, size_t* smem) {
   const int tot = a.nplanes[0] + a.nplanes[1] + a.nplanes[2];
-  if (tot == 0) return;
-  dim3 grid(d.ngz, tot);
+  *grid = tot == 0 ? dim3(0, 0, 0) : dim3(d.ngz, tot);
   const int hp = d.ngx / 2 + 1;
-  size_t sm = sizeof(cpx_t<R>) * sx_elems<R>(2 * (size_t)hp) + sizeof(R) * 2 * (size_t)d.ngx;
+  *smem = sizeof(cpx_t<R>) * sx_elems<R>(2 * (size_t)hp) + sizeof(R) * 2 * (size_t)d.ngx;
+}
+
+template <typename R>
+void launch_xmask(const MaskArgs<R>& a, const Dims& d, const FftPlan& ph, const double2* rtw, cudaStream_t st) {
+  dim3 grid;
+  size_t sm;
+  xmask_shape(a, d, &grid, &sm);
+  if (grid.x == 0) return;
   k_xmask<R><<<grid, 128, sm, st>>>(a, d, ph, rtw);
 }
 
@@ -459,10 +526,10 @@ __device__ __forceinline__ double2 nterm(float2 A, float2 B, float2 D1, float2 D
 }
 
 template <typename P>
-__global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void assemble_body(const AsmArgs& a, const Dims& d, const Tables& t, int bx, int by) {
+  const int col = bx * blockDim.x + threadIdx.x;
   if (col >= d.np) return;
-  const int jj = blockIdx.y;
+  const int jj = by;
   const int np = d.np;
   const int i = col % d.nkx, kk = col / d.nkx;
   const double kx = t.kx[i], kz = t.kz[kk], k2 = t.k2x[i] + t.k2z[kk];
@@ -553,6 +620,12 @@ __global__ void __launch_bounds__(256) k_assemble(AsmArgs a, Dims d, Tables t) {
   }
 }
 
+template <typename P>
+__global__ void __launch_bounds__(256) k_assemble(const __grid_constant__ AsmArgs a, const __grid_constant__ Dims d,
+                                                  const __grid_constant__ Tables t) {
+  assemble_body<P>(a, d, t, blockIdx.x, blockIdx.y);
+}
+
 void launch_assemble(const AsmArgs& a, const Dims& d, const Tables& t, cudaStream_t st) {
   dim3 grid((d.np + 255) / 256, d.nyu);
   if (a.p32[0]) k_assemble<float2><<<grid, 256, 0, st>>>(a, d, t);
@@ -608,11 +681,11 @@ __device__ __forceinline__ void thomas_column(double2* __restrict__ R, double2* 
 // Velocity solves: one thread per (component, column).  Long columns use the
 // LU of the whole channel; short columns solve their two wall bands with those
 // bands' LUs and are zero in between.
-__global__ void __launch_bounds__(128) k_vsolve(double2* r1, double2* r2, double2* r3, double2* u1, double2* u2,
-                                                double2* u3, Dims d, Tables t, int k) {
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void vsolve_body(double2* r1, double2* r2, double2* r3, double2* u1, double2* u2, double2* u3,
+                                            const Dims& d, const Tables& t, int k, int bx, int by) {
+  const int col = bx * blockDim.x + threadIdx.x;
   if (col >= d.np) return;
-  const int comp = blockIdx.y;
+  const int comp = by;
   const int ny = comp == 1 ? d.nyv : d.nyu;
   double2* R = comp == 0 ? r1 : (comp == 1 ? r2 : r3);
   double2* U = comp == 0 ? u1 : (comp == 1 ? u2 : u3);
@@ -631,6 +704,12 @@ __global__ void __launch_bounds__(128) k_vsolve(double2* r1, double2* r2, double
   for (int jj = e1 + 1; jj < s3; ++jj) U[(size_t)jj * np + col] = double2{0.0, 0.0};
 }
 
+__global__ void __launch_bounds__(128) k_vsolve(double2* r1, double2* r2, double2* r3, double2* u1, double2* u2,
+                                                double2* u3, const __grid_constant__ Dims d,
+                                                const __grid_constant__ Tables t, int k) {
+  vsolve_body(r1, r2, r3, u1, u2, u3, d, t, k, blockIdx.x, blockIdx.y);
+}
+
 void launch_vsolve(double2* r1, double2* r2, double2* r3, double2* u1, double2* u2, double2* u3, const Dims& d,
                    const Tables& t, int k, cudaStream_t st) {
   dim3 grid((d.np + 127) / 128, 3);
@@ -639,7 +718,8 @@ void launch_vsolve(double2* r1, double2* r2, double2* r3, double2* u1, double2* 
 
 // flowrate_corr on mode (0,0): the flow-rate sum runs in the reference's
 // order on one thread; the correction is spread over the block.
-__global__ void k_flowrate(double2* u1, DevScalars* sc, Dims d, Tables t, int k, double Qx1) {
+__device__ __forceinline__ void flowrate_body(double2* u1, DevScalars* sc, const Dims& d, const Tables& t, int k,
+                                              double Qx1) {
   __shared__ double gsh;
   if (threadIdx.x == 0) {
     double Q = 0.0;
@@ -656,6 +736,11 @@ __global__ void k_flowrate(double2* u1, DevScalars* sc, Dims d, Tables t, int k,
     double2* u = u1 + (size_t)(j - d.ju0) * d.np;
     u->x = u->x + g * u11[j];
   }
+}
+
+__global__ void k_flowrate(double2* u1, DevScalars* sc, const __grid_constant__ Dims d, const __grid_constant__ Tables t,
+                           int k, double Qx1) {
+  flowrate_body(u1, sc, d, t, k, Qx1);
 }
 
 void launch_flowrate(double2* u1, DevScalars* sc, const Dims& d, const Tables& t, int k, double Qx1, cudaStream_t st) {
@@ -803,10 +888,10 @@ __device__ __forceinline__ void psolve_segment(double2* __restrict__ u1, double2
   }
 }
 
-__global__ void __launch_bounds__(128, 4) k_psolve(double2* u1, double2* u2, double2* u3, double2* p, double2* psi,
-                                                Dims d, Tables t, double dtirk, double dtrk, double gwb,
-                                                double gwt, DevScalars* sc) {
-  const int col = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void psolve_body(double2* u1, double2* u2, double2* u3, double2* p, double2* psi, const Dims& d,
+                                            const Tables& t, double dtirk, double dtrk, double gwb, double gwt,
+                                            DevScalars* sc, int bx) {
+  const int col = bx * blockDim.x + threadIdx.x;
   if (col >= d.np) return;
   const size_t np = d.np;
   const int i = col % d.nkx, kk = col / d.nkx;
@@ -832,6 +917,12 @@ __global__ void __launch_bounds__(128, 4) k_psolve(double2* u1, double2* u2, dou
     u3[(size_t)(d.nyu - 1) * np + col] = double2{-gwt * wt.x, -gwt * wt.y};
   }
   if (bad && sc) atomicOr(&sc->err, kErrNonFinite);
+}
+
+__global__ void __launch_bounds__(128, 4) k_psolve(double2* u1, double2* u2, double2* u3, double2* p, double2* psi,
+                                                   const __grid_constant__ Dims d, const __grid_constant__ Tables t,
+                                                   double dtirk, double dtrk, double gwb, double gwt, DevScalars* sc) {
+  psolve_body(u1, u2, u3, p, psi, d, t, dtirk, dtrk, gwb, gwt, sc, blockIdx.x);
 }
 
 void launch_psolve(double2* u1, double2* u2, double2* u3, double2* p, double2* psi, const Dims& d, const Tables& t,
@@ -1168,6 +1259,111 @@ void launch_spectra(const double2* u1, const double2* u2, const double2* u3, con
   k_spectra<<<grid, 256, 0, st>>>(u1, u2, u3, p, sp, d, t);
 }
 
+// ---------------------------------------------------------------------------
+// Batched kernels (several solvers per launch, lh_internal.h)
+// ---------------------------------------------------------------------------
+
+// The batched kernels read their member's arguments with a block-uniform index into the parameter bank, which
+// costs registers the single launches do not need; their launch bounds cap the registers at the single
+// launches' counts, so that as many CTAs fit on an SM.
+
+// member owning block b (members are few; the scan is uniform across the block)
+template <typename D>
+__device__ __forceinline__ int batch_member(const Batch<D>& b, int blk) {
+  int m = 0;
+  while (m + 1 < b.n && blk >= b.start[m + 1]) ++m;
+  return m;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 8 : 5) k_zinv_batch(const __grid_constant__ Batch<ZDesc<R>> b) {
+  const int m = batch_member(b, blockIdx.x);
+  const ZDesc<R>& D = b.desc[m];
+  const int q = blockIdx.x - b.start[m], gxy = D.gx * D.gy;
+  zinv_body<R>(D.jobs, D.d, D.p, D.tx, q % D.gx, (q % gxy) / D.gx, q / gxy);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 8 : 5) k_zfwd_batch(const __grid_constant__ Batch<ZDesc<R>> b) {
+  const int m = batch_member(b, blockIdx.x);
+  const ZDesc<R>& D = b.desc[m];
+  const int q = blockIdx.x - b.start[m], gxy = D.gx * D.gy;
+  zfwd_body<R>(D.jobs, D.d, D.p, D.tx, D.scale, q % D.gx, (q % gxy) / D.gx, q / gxy);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 6 : 5) k_xprod_batch(const __grid_constant__ Batch<XDesc<R>> b) {
+  const int m = batch_member(b, blockIdx.x);
+  const XDesc<R>& D = b.desc[m];
+  const int q = blockIdx.x - b.start[m];
+  xprod_body<R>(D.a, D.d, D.ph, D.pf, D.rtw, q % D.gx, q / D.gx);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 16 : 9) k_xmask_batch(const __grid_constant__ Batch<MDesc<R>> b) {
+  const int m = batch_member(b, blockIdx.x);
+  const MDesc<R>& D = b.desc[m];
+  const int q = blockIdx.x - b.start[m];
+  xmask_body<R>(D.a, D.d, D.ph, D.rtw, q % D.gx, q / D.gx);
+}
+
+template <typename P>
+__global__ void __launch_bounds__(256, 3) k_assemble_batch(const __grid_constant__ Batch<ADesc> b) {
+  const int m = batch_member(b, blockIdx.x);
+  const ADesc& D = b.desc[m];
+  const int q = blockIdx.x - b.start[m];
+  assemble_body<P>(D.a, D.d, D.t, q % D.gx, q / D.gx);
+}
+
+__global__ void __launch_bounds__(128) k_vsolve_batch(const __grid_constant__ Batch<VDesc> b) {
+  const int m = batch_member(b, blockIdx.x);
+  const VDesc& D = b.desc[m];
+  const int q = blockIdx.x - b.start[m];
+  vsolve_body(D.r1, D.r2, D.r3, D.u1, D.u2, D.u3, D.d, D.t, D.k, q % D.gx, q / D.gx);
+}
+
+__global__ void k_flowrate_batch(const __grid_constant__ Batch<FDesc> b) {
+  const FDesc& D = b.desc[batch_member(b, blockIdx.x)];
+  flowrate_body(D.u1, D.sc, D.d, D.t, D.k, D.Qx1);
+}
+
+__global__ void __launch_bounds__(128, 4) k_psolve_batch(const __grid_constant__ Batch<PDesc> b) {
+  const int m = batch_member(b, blockIdx.x);
+  const PDesc& D = b.desc[m];
+  psolve_body(D.u1, D.u2, D.u3, D.p, D.psi, D.d, D.t, D.dtirk, D.dtrk, D.gwb, D.gwt, D.sc, blockIdx.x - b.start[m]);
+}
+
+template <typename R>
+void launch_zinv_batch(const Batch<ZDesc<R>>& b, size_t smem, cudaStream_t st) {
+  if (b.n > 0 && b.start[b.n] > 0) k_zinv_batch<R><<<b.start[b.n], 256, smem, st>>>(b);
+}
+template <typename R>
+void launch_zfwd_batch(const Batch<ZDesc<R>>& b, size_t smem, cudaStream_t st) {
+  if (b.n > 0 && b.start[b.n] > 0) k_zfwd_batch<R><<<b.start[b.n], 256, smem, st>>>(b);
+}
+template <typename R>
+void launch_xprod_batch(const Batch<XDesc<R>>& b, size_t smem, cudaStream_t st) {
+  if (b.n > 0 && b.start[b.n] > 0) k_xprod_batch<R><<<b.start[b.n], 256, smem, st>>>(b);
+}
+template <typename R>
+void launch_xmask_batch(const Batch<MDesc<R>>& b, size_t smem, cudaStream_t st) {
+  if (b.n > 0 && b.start[b.n] > 0) k_xmask_batch<R><<<b.start[b.n], 128, smem, st>>>(b);
+}
+void launch_assemble_batch(const Batch<ADesc>& b, bool fp32_products, cudaStream_t st) {
+  if (b.n <= 0 || b.start[b.n] <= 0) return;
+  if (fp32_products) k_assemble_batch<float2><<<b.start[b.n], 256, 0, st>>>(b);
+  else k_assemble_batch<double2><<<b.start[b.n], 256, 0, st>>>(b);
+}
+void launch_vsolve_batch(const Batch<VDesc>& b, cudaStream_t st) {
+  if (b.n > 0 && b.start[b.n] > 0) k_vsolve_batch<<<b.start[b.n], 128, 0, st>>>(b);
+}
+void launch_flowrate_batch(const Batch<FDesc>& b, cudaStream_t st) {
+  if (b.n > 0 && b.start[b.n] > 0) k_flowrate_batch<<<b.start[b.n], 256, 0, st>>>(b);
+}
+void launch_psolve_batch(const Batch<PDesc>& b, cudaStream_t st) {
+  if (b.n > 0 && b.start[b.n] > 0) k_psolve_batch<<<b.start[b.n], 128, 0, st>>>(b);
+}
+
 // FP64 FMA throughput probe: every thread runs eight independent dependent
 // chains of fma(x, a, b), enough independent work to keep the FP64 pipe busy;
 // the sum is stored only if it equals an impossible value, so no chain is
@@ -1238,10 +1434,14 @@ cudaError_t configure_kernels() {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  const cudaError_t r[9] = {allow_smem(k_xcond, optin), allow_smem(k_zinv<double>, optin), allow_smem(k_zinv<float>, optin),
-                            allow_smem(k_zfwd<double>, optin), allow_smem(k_zfwd<float>, optin),
-                            allow_smem(k_xprod<double>, optin), allow_smem(k_xprod<float>, optin),
-                            allow_smem(k_xmask<double>, optin), allow_smem(k_xmask<float>, optin)};
+  const cudaError_t r[17] = {allow_smem(k_xcond, optin), allow_smem(k_zinv<double>, optin), allow_smem(k_zinv<float>, optin),
+                             allow_smem(k_zfwd<double>, optin), allow_smem(k_zfwd<float>, optin),
+                             allow_smem(k_xprod<double>, optin), allow_smem(k_xprod<float>, optin),
+                             allow_smem(k_xmask<double>, optin), allow_smem(k_xmask<float>, optin),
+                             allow_smem(k_zinv_batch<double>, optin), allow_smem(k_zinv_batch<float>, optin),
+                             allow_smem(k_zfwd_batch<double>, optin), allow_smem(k_zfwd_batch<float>, optin),
+                             allow_smem(k_xprod_batch<double>, optin), allow_smem(k_xprod_batch<float>, optin),
+                             allow_smem(k_xmask_batch<double>, optin), allow_smem(k_xmask_batch<float>, optin)};
   for (cudaError_t x : r)
     if (x != cudaSuccess) return x;
   if (dev < 64) done |= 1ull << dev;
@@ -1258,6 +1458,20 @@ template void launch_xprod<float>(const ProdArgs<float>&, const Dims&, const Fft
                                   cudaStream_t);
 template void launch_xmask<double>(const MaskArgs<double>&, const Dims&, const FftPlan&, const double2*, cudaStream_t);
 template void launch_xmask<float>(const MaskArgs<float>&, const Dims&, const FftPlan&, const double2*, cudaStream_t);
+template void zpass_shape<double>(const ZJobs<double>&, const Dims&, int, dim3*, size_t*);
+template void zpass_shape<float>(const ZJobs<float>&, const Dims&, int, dim3*, size_t*);
+template void xprod_shape<double>(const ProdArgs<double>&, const Dims&, dim3*, size_t*);
+template void xprod_shape<float>(const ProdArgs<float>&, const Dims&, dim3*, size_t*);
+template void xmask_shape<double>(const MaskArgs<double>&, const Dims&, dim3*, size_t*);
+template void xmask_shape<float>(const MaskArgs<float>&, const Dims&, dim3*, size_t*);
+template void launch_zinv_batch<double>(const Batch<ZDesc<double>>&, size_t, cudaStream_t);
+template void launch_zinv_batch<float>(const Batch<ZDesc<float>>&, size_t, cudaStream_t);
+template void launch_zfwd_batch<double>(const Batch<ZDesc<double>>&, size_t, cudaStream_t);
+template void launch_zfwd_batch<float>(const Batch<ZDesc<float>>&, size_t, cudaStream_t);
+template void launch_xprod_batch<double>(const Batch<XDesc<double>>&, size_t, cudaStream_t);
+template void launch_xprod_batch<float>(const Batch<XDesc<float>>&, size_t, cudaStream_t);
+template void launch_xmask_batch<double>(const Batch<MDesc<double>>&, size_t, cudaStream_t);
+template void launch_xmask_batch<float>(const Batch<MDesc<float>>&, size_t, cudaStream_t);
 
 }  // namespace lh
 

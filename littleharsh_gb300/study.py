@@ -480,6 +480,22 @@ def precision_ensemble(cfg: dict, realisations: int = 3, re_tau: float = 180.0, 
         arr = np.array([p[k][m] for p in fp_p])
         sd = arr.std(axis=0, ddof=1) if len(fp_p) > 1 else np.zeros(arr.shape[1])
         sem[k] = float(np.max(sd) / np.sqrt(len(fp_p)) / np.max(np.abs(fpm[k][m])))
+    # the noise of a difference of two means: both groups' spreads, pointwise in y, at the point where the
+    # difference is largest; and the difference seed by seed (a mixed run against the FP64 run from its field)
+    diff_z, per_seed = {}, {}
+    n = len(fp_p)
+    for k in PROFILE_KEYS:
+        m = masks[_GRID[k][0]]
+        a = np.array([p[k][m] for p in fp_p])
+        b = np.array([p[k][m] for p in mx_p])
+        scale = np.max(np.abs(fpm[k][m]))
+        d = b.mean(axis=0) - a.mean(axis=0)
+        i = int(np.argmax(np.abs(d)))
+        if n > 1:
+            se = np.sqrt((a.std(axis=0, ddof=1) ** 2 + b.std(axis=0, ddof=1) ** 2) / n)
+            diff_z[k] = {"diff": float(d[i] / scale), "se_diff": float(se[i] / scale),
+                         "z": float(d[i] / se[i]) if se[i] > 0 else None}
+        per_seed[k] = [float((b[q][i] - a[q][i]) / scale) for q in range(n)]
     tke_avg = []
     for i in range(len(sols)):
         rr = [r for r in run.records[i] if r["t"] >= t_spin]
@@ -487,7 +503,8 @@ def precision_ensemble(cfg: dict, realisations: int = 3, re_tau: float = 180.0, 
     res = {"grid": [sols[0].ngx, sols[0].ngz, sols[0].nyu], "realisations": realisations, "seeds": [seed + q for q in range(realisations)],
            "steps": run.steps, "t_end": sols[0].time()["t"], "avg_turnovers": (sols[0].time()["t"] - t_spin) / T,
            "mean_profile_err_mixed_vs_fp64": err, "max_mean_profile_err": max(err.values()),
-           "fp64_mean_standard_error": sem, "tke_fp64": tke_avg[0::2], "tke_mixed": tke_avg[1::2],
+           "fp64_mean_standard_error": sem, "difference_at_its_largest": diff_z,
+           "per_seed_difference_at_that_point": per_seed, "tke_fp64": tke_avg[0::2], "tke_mixed": tke_avg[1::2],
            "gpu_ms_per_ensemble_step": run.gpu_ms / max(run.steps, 1),
            "profiles": {"y_u": run.grids["u"].tolist(), "fp64_mean": {k: v.tolist() for k, v in fpm.items()},
                         "mixed_mean": {k: v.tolist() for k, v in mxm.items()}}}
