@@ -315,7 +315,10 @@ def main(argv=None):
     p.add_argument("--max-seconds", type=float, default=1e30, help="end the run early (wall clock)")
     p.add_argument("--out", required=True)
     q = sub.add_parser("warmstart", help="learned warm start on configuration 1's geometry")
-    q.add_argument("--grid", choices=("config1",), default="config1")
+    q.add_argument("--grid", choices=("config1", "config1x2"), default="config1",
+                   help="config1: fine configuration 1, coarse at half its resolution; config1x2: fine at twice "
+                        "configuration 1's resolution, coarse configuration 1")
+    q.add_argument("--precision", choices=("fp64", "mixed"), default="fp64")
     q.add_argument("--spinup-turnovers", type=float, default=15.0)
     q.add_argument("--eval-turnovers", type=float, default=15.0)
     q.add_argument("--snapshots", type=int, default=200)
@@ -361,15 +364,17 @@ def main(argv=None):
             json.dump(res, f)
     elif a.cmd == "warmstart":
         from . import warmstart
-        from .workloads import CONFIG1_COARSE
-        res = warmstart.experiment(CONFIG1, CONFIG1_COARSE, RE_TAU["config1"], spinup_turnovers=a.spinup_turnovers,
+        from .workloads import CONFIG1_COARSE, CONFIG1_X2
+        fine, coarse = (CONFIG1, CONFIG1_COARSE) if a.grid == "config1" else (CONFIG1_X2, CONFIG1)
+        res = warmstart.experiment(fine, coarse, RE_TAU["config1"], spinup_turnovers=a.spinup_turnovers,
                                    snapshots=a.snapshots, snap_every=a.snap_every, train_epochs=a.epochs,
                                    eval_turnovers=a.eval_turnovers, window=a.window, avg_windows=a.avg_windows,
                                    seed=a.seed, max_steps=a.max_steps, realisations=a.realisations,
-                                   log=lambda m: print(m, flush=True))
+                                   precision=1 if a.precision == "mixed" else 0, log=lambda m: print(m, flush=True))
         with open(a.out, "w") as f:
             json.dump(res, f, default=float)
         print(json.dumps({"starts": {k: v["stationary_steps"] for k, v in res["starts"].items()},
+                          "first_within": {k: v["first_within_steps"] for k, v in res["starts"].items()},
                           "tol_effective": res["reference_run"]["tol_effective"],
                           "val": res["training"]["history"][-1]}))
 

@@ -325,7 +325,7 @@ def experiment(fine_cfg: dict, coarse_cfg: dict, re_tau: float, spinup_turnovers
                snapshots: int = 200, snap_every: int = 100, train_epochs: int = 20, eval_turnovers: float = 15.0,
                window: int = 200, every: int = 10, avg_windows: int = 10, tol: float = 0.005, cfl: float = 0.5,
                lr: float = 1e-3, seed: int = 1, max_steps: int = 2_000_000, realisations: int = 1,
-               log=None) -> dict:
+               precision: int = 0, log=None) -> dict:
     """The learned warm start end to end on one fine/coarse grid pair.
 
     1. fine run from the seeded laminar + noise start: spin-up, then the
@@ -338,6 +338,7 @@ def experiment(fine_cfg: dict, coarse_cfg: dict, re_tau: float, spinup_turnovers
        seeds and coarse runs); steps until each run's statistics stay within
        `tol` (or the noise floor of the converged statistics, if larger) of
        the converged ones.
+    Every solver runs in `precision` (LH_PREC_FP64 or LH_PREC_MIXED).
     """
     import littleharsh_gb300 as lh
     from . import study
@@ -346,8 +347,9 @@ def experiment(fine_cfg: dict, coarse_cfg: dict, re_tau: float, spinup_turnovers
     res = {"fine": fine_cfg, "coarse": coarse_cfg, "turnover_time": T}
 
     # 1. fine spin-up, converged statistics, snapshots
-    fine = lh.Solver(lh.Config(**fine_cfg))
+    fine = lh.Solver(lh.Config(**fine_cfg), precision=precision)
     fgi = GridInfo(fine)
+    t_phase = time.perf_counter()
     dt0 = study.seeded_start([fine], seed, cfl)
     qxt = fine.time()["QxT"]
     run = study.LongRun([fine], cfl=cfl, window=window, every=every)
@@ -389,6 +391,7 @@ def experiment(fine_cfg: dict, coarse_cfg: dict, re_tau: float, spinup_turnovers
     tol_eff = max(tol, floor)
     fine_devs = study.deviation_series(recs, ref_prof, ref_mpgx, fine.ngx, fine.ngz, run.grids, avg_windows)
     res["reference_run"] = {"dt0": dt0, "steps": run.steps, "t": fine.time()["t"], "spinup_windows": spin_windows,
+                            "seconds": time.perf_counter() - t_phase,
                             "snapshot_seconds": time.perf_counter() - t_snap0, "ref_mpgx": ref_mpgx,
                             "noise_floor": floor, "tol": tol, "tol_effective": tol_eff,
                             "plain_start_stationary_step": study.stationary_from(recs, fine_devs, tol_eff,
@@ -400,7 +403,7 @@ def experiment(fine_cfg: dict, coarse_cfg: dict, re_tau: float, spinup_turnovers
     fine.close()
 
     # 2. coarse runs (one per realisation) to stationary fields, advanced together
-    coarses = [lh.Solver(lh.Config(**coarse_cfg)) for _ in range(realisations)]
+    coarses = [lh.Solver(lh.Config(**coarse_cfg), precision=precision) for _ in range(realisations)]
     for q, c in enumerate(coarses):
         study.seeded_start([c], seed + 1 + 10 * q, cfl)
     crun = study.LongRun(coarses, cfl=cfl, window=window, every=every)
@@ -428,7 +431,7 @@ def experiment(fine_cfg: dict, coarse_cfg: dict, re_tau: float, spinup_turnovers
     sols, kinds = [], []
     for q in range(realisations):
         for kind in names:
-            s_ = lh.Solver(lh.Config(**fine_cfg))
+            s_ = lh.Solver(lh.Config(**fine_cfg), precision=precision)
             if kind == "laminar_noise":
                 study.seeded_start([s_], seed + 2 + 10 * q, cfl)
             else:
@@ -443,7 +446,9 @@ def experiment(fine_cfg: dict, coarse_cfg: dict, re_tau: float, spinup_turnovers
         tm = s_.time()
         s_.set_time(0.0, dt_common, tm["mpgx"], qxt)
     erun = study.LongRun(sols, cfl=cfl, window=window, every=every)
+    t_eval = time.perf_counter()
     run_until(erun, eval_turnovers * T, max_steps, log=log, tag="starts")
+    res["eval_seconds"] = time.perf_counter() - t_eval
     starts = {k: {"runs": []} for k in names}
     for i, kind in enumerate(kinds):
         rr = erun.records[i]

@@ -33,6 +33,10 @@ XZ576_NY49 = dict(CONFIG2, ny=49, dsty=4)
 # learned warm start on configuration 1's geometry (posts 1 x 2 points)
 CONFIG1_COARSE = dict(CONFIG1, ngalx=48, ngalz=48, ny=49, dsty=8, dstx=1, dstz=2)
 
+# configuration 1 at twice its resolution in x, z and y (128 x 128 modes, ny 193, posts 4 x 8 points): the fine
+# grid of the warm start whose coarse grid is configuration 1 itself, a resolved DNS grid at Re_tau 180
+CONFIG1_X2 = dict(CONFIG1, ngalx=192, ngalz=192, ny=193, dsty=32, dstx=4, dstz=8)
+
 # configuration 5: configuration 1's flow and canopy (12 x 6 posts, h = 0.2, a
 # quarter of the pitch wide) on the 384 x 385 x 384 fine grid and the
 # 128 x 193 x 128 coarse grid (modes x ny x modes)
