@@ -59,6 +59,14 @@ int lh_sr_tc_status(int32_t* timed_out);
 int lh_sr_conv_wgrad(int32_t cin, int32_t cout, const void* in, const void* dout, float* dw, float* db, int32_t X,
                      int32_t Y, int32_t Z, void* stream);
 
+/* The same weight and bias gradients on the tcgen05 tensor cores: MMAs whose
+ * reduction runs over 16 z voxels, both operands read as they lie in memory
+ * (MN-major shared-memory layouts), fp32 accumulators in TMEM for the whole
+ * persistent CTA, added to dw once.  Z must also be a multiple of 16.  A wait
+ * that runs out is recorded for lh_sr_tc_status. */
+int lh_sr_conv_wgrad_tc(int32_t cin, int32_t cout, const void* in, const void* dout, float* dw, float* db,
+                        int32_t X, int32_t Y, int32_t Z, void* stream);
+
 /* wt[tap][ci][co] = w[26 - tap][co][ci]: with these weights lh_sr_conv_fwd(cout, cin, ...)
  * computes the data gradient of the convolution. */
 int lh_sr_flip_weights(int32_t cin, int32_t cout, const void* w, void* wt, void* stream);

@@ -34,7 +34,7 @@ EXPORTED_SYMBOLS = [
     "lh_project_noalloc", "lh_set_monitor", "lh_get_monitor", "lh_fp64_peak", "lh_ensemble_create", "lh_ensemble_step", "lh_ensemble_last_error",
     "lh_ensemble_free", "lh_ensemble_set_mode", "lh_ensemble_info", "lh_autotune", "lh_get_launch_shapes", "lh_write_restart", "lh_read_restart", "lh_write_stats", "lh_write_spectra", "lh_read_input", "lh_setup_grid", "lh_setup_canopy",
     # include/lh_srnet.h: kernels of the learned warm start
-    "lh_sr_conv_fwd", "lh_sr_conv_fwd_tc", "lh_sr_tc_status", "lh_sr_conv_wgrad", "lh_sr_flip_weights", "lh_sr_mse", "lh_sr_adam",
+    "lh_sr_conv_fwd", "lh_sr_conv_fwd_tc", "lh_sr_tc_status", "lh_sr_conv_wgrad", "lh_sr_conv_wgrad_tc", "lh_sr_flip_weights", "lh_sr_mse", "lh_sr_adam",
 ]
 
 
@@ -149,6 +149,7 @@ def load_library(build: bool = True) -> C.CDLL:
     L.lh_sr_conv_fwd_tc.argtypes = [i32, i32, vp, vp, vp, vp, i32, vp, vp, i32, i32, i32, i32, vp]
     L.lh_sr_tc_status.argtypes = [C.POINTER(i32)]
     L.lh_sr_conv_wgrad.argtypes = [i32, i32, vp, vp, vp, vp, i32, i32, i32, vp]
+    L.lh_sr_conv_wgrad_tc.argtypes = [i32, i32, vp, vp, vp, vp, i32, i32, i32, vp]
     L.lh_sr_flip_weights.argtypes = [i32, i32, vp, vp, vp]
     L.lh_sr_mse.argtypes = [vp, vp, vp, vp, vp, C.c_int64, vp]
     L.lh_sr_adam.argtypes = [vp, vp, vp, vp, vp, i32] + [C.c_float] * 5 + [i32, vp]

@@ -673,6 +673,259 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (warp == TC_MMA_WARP) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;\n" ::"r"(tmem));
 }
 
+// ---- weight gradient on tcgen05 -------------------------------------------------
+//
+// dW[tap][co][ci] = sum_v dout[v][co] in[v + off(tap)][ci] with the reduction (K) over 16 consecutive z voxels
+// per MMA.  One operand, S, has 32 channels and is read at shifted voxels; the other, U (Cu = 16 or 32
+// channels), at the tile's own voxels and at the levels above and below.  For the 32 -> Cout layers S is the
+// input and U the output gradient; for the 16 -> 32 layer S is the output gradient and U the input, and the
+// taps come out mirrored (sum_v dout[v] in[v + t] = sum_u dout[u - t] in[u]).
+//
+// Both operands are MN-major: a core matrix is 8 consecutive z voxels (K) x 8 channels (16 bytes), which is
+// how channels-last volumes arrive, so cp.async copies 16-byte chunks straight into place.
+//   A (M = 128): rows (l, c) = channel c of S on x line x + l - 1, l = 0..3 (l = 3 is a spare line whose
+//     rows are discarded), at z + dz - 1.  S halo rows [level][line][chunk][z - 1 .. z + 16] with the line
+//     pitch = 4 chunk planes, so the 16 core matrices of rows (l, chunk) sit one plane pitch apart; the z tap
+//     dz is the descriptor's start address moved dz rows.
+//   B (N = 3 Cu): columns (e, c) = channel c of U at level y + e - 1, e = 0..2, the levels a level pitch
+//     apart in U's rows [column][level][chunk][z].
+// One MMA per (level of the tile, x column, dz) accumulates D[dz] (128 x 3Cu fp32 in TMEM) over every tile
+// of the persistent CTA; tap (dy, dz, dx) of D[dz][(l, c)][(e, c')] is (1 - e, dz - 1, l - 1) relative to U.
+// Roles as in the forward kernel: warps 0-3 copy a tile's halo into a ring of stage buffers and arrive on
+// `full`; warp 8 (one thread) issues the tile's MMAs and commits them to `empty`; warps 4-7 sum the tile's
+// output gradient (the bias gradient) from the same buffer and arrive on `empty` too, and at the end read
+// D from TMEM and add it to dw.  Every wait is bounded as in the forward kernel.
+constexpr int WT_TXW = 8;               // x columns per tile
+constexpr int WT_TY = 2;                // y levels per tile
+constexpr int WT_TZ = 16;               // z voxels per tile = the K of one MMA
+constexpr int WT_L = WT_TXW + 3;        // S halo lines x0 - 1 .. x0 + 9
+constexpr int WT_ZR = WT_TZ + 2;        // S halo z rows
+constexpr int WT_ZP = 19;               // S z pitch in 16-byte rows (odd: a warp's copies spread over all banks)
+constexpr int WT_ZPU = 17;              // U z pitch
+constexpr int WT_LAG = 2;
+constexpr int WT_THREADS = 288;
+
+template <int CU>
+struct WtGeom {
+  static constexpr int KCS = 4, KCU = CU / 8, UL = WT_TY + 2;
+  static constexpr int SROWS = WT_TY * WT_L * KCS * WT_ZP;  // S halo rows of a stage
+  static constexpr int XIP = UL * KCU * WT_ZPU + 1;         // U rows per x column (odd)
+  static constexpr int BUF = SROWS + WT_TXW * XIP;          // 16-byte rows per stage
+  static constexpr int NBUF = CU == 32 ? 3 : 4;
+  static constexpr int NCOL = 3 * CU;                       // N of one MMA
+  static constexpr int TCOLS = 3 * NCOL <= 256 ? 256 : 512; // TMEM columns (a power of two >= 3 NCOL)
+  static constexpr size_t smem = (size_t)NBUF * BUF * 16 + (2 * NBUF + 1) * 8 + 16;
+};
+
+template <int CU, bool SWAP>
+__global__ void __launch_bounds__(WT_THREADS, 1)
+    k_conv_wgrad_tc(const __nv_bfloat16* __restrict__ sop, const __nv_bfloat16* __restrict__ uop,
+                    float* __restrict__ dw, float* __restrict__ db, Vol v, int* __restrict__ err) {
+  using G = WtGeom<CU>;
+  constexpr int KCS = G::KCS, KCU = G::KCU, NBUF = G::NBUF, BUF = G::BUF, NCOL = G::NCOL;
+  constexpr int CIN = SWAP ? CU : 32, COUT = SWAP ? 32 : CU;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint4* ring = reinterpret_cast<uint4*>(smem_raw);  // [NBUF][BUF]
+  uint64_t* full = reinterpret_cast<uint64_t*>(ring + (size_t)NBUF * BUF);
+  uint64_t* empty = full + NBUF;
+  uint64_t* done = empty + NBUF;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+  volatile int* abort = reinterpret_cast<volatile int*>(tslot + 1);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < NBUF; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(full + b)), "r"(TC_PRODUCERS));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 5;\n" ::"r"(smem_u32(empty + b)));  // MMAs + 4 warps
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(done)));
+    *abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == TC_MMA_WARP) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tslot)),
+                 "n"(G::TCOLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *tslot;
+
+  const int nty = (v.Y + WT_TY - 1) / WT_TY, ntz = v.Z / WT_TZ, ntx = v.X / WT_TXW;
+  const int ntiles = nty * ntz * ntx;
+  const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  auto tile_origin = [&](int s, int& y0, int& z0, int& x0) {
+    const int tile = blockIdx.x + s * gridDim.x;
+    const int xt = tile % ntx, rest = tile / ntx;
+    x0 = xt * WT_TXW;
+    z0 = (rest % ntz) * WT_TZ;
+    y0 = (rest / ntz) * WT_TY;
+  };
+
+  if (warp < 4) {
+    // ---- producers: tile s into buffer s % NBUF
+    const int p = threadIdx.x;
+    auto land = [&](int st) {
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      tc_arrive(full + st % NBUF);
+    };
+    int s = 0;
+    for (; s < my_tiles; ++s) {
+      if (s >= NBUF && !tc_wait(empty + s % NBUF, (uint32_t)((s / NBUF - 1) & 1), abort)) break;
+      int y0, z0, x0;
+      tile_origin(s, y0, z0, x0);
+      uint4* buf = ring + (size_t)(s % NBUF) * BUF;
+      // S: rows ((t L + line) 4 + chunk) ZP + zr; levels y0 + t past the top are zeros
+      for (int c = p; c < WT_TY * WT_ZR * WT_L * KCS; c += TC_PRODUCERS) {
+        const int kc = c % KCS, line = (c / KCS) % WT_L, r2 = c / (KCS * WT_L);
+        const int zr = r2 % WT_ZR, t = r2 / WT_ZR;
+        const int gy = y0 + t;
+        const bool ok = gy < v.Y;
+        int gz = z0 + zr - 1, gx = x0 + line - 1;
+        gz = gz < 0 ? gz + v.Z : (gz >= v.Z ? gz - v.Z : gz);
+        gx = gx < 0 ? gx + v.X : (gx >= v.X ? gx - v.X : gx);
+        const size_t vox = ok ? ((size_t)gy * v.Z + gz) * v.X + gx : 0;
+        cp_async16(buf + ((size_t)(t * WT_L + line) * KCS + kc) * WT_ZP + zr, sop + vox * 32 + kc * 8, ok);
+      }
+      // U: rows SROWS + column XIP + (level KCU + chunk) ZPU + z; levels y0 - 1 .. y0 + 2, zeros outside
+      for (int c = p; c < G::UL * WT_TZ * WT_TXW * KCU; c += TC_PRODUCERS) {
+        const int kcu = c % KCU, xi = (c / KCU) % WT_TXW, r2 = c / (KCU * WT_TXW);
+        const int z = r2 % WT_TZ, lev = r2 / WT_TZ;
+        const int gy = y0 + lev - 1;
+        const bool ok = gy >= 0 && gy < v.Y;
+        const size_t vox = ok ? ((size_t)gy * v.Z + z0 + z) * v.X + x0 + xi : 0;
+        cp_async16(buf + G::SROWS + (size_t)xi * G::XIP + (lev * KCU + kcu) * WT_ZPU + z, uop + vox * CU + kcu * 8,
+                   ok);
+      }
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+      if (s >= WT_LAG) {
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(WT_LAG) : "memory");
+        land(s - WT_LAG);
+      }
+    }
+    if (s == my_tiles) {
+      for (int q = my_tiles - WT_LAG < 0 ? 0 : my_tiles - WT_LAG; q < my_tiles; ++q) {
+        if (my_tiles - 1 - q >= 1) asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        else asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        land(q);
+      }
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  } else if (warp == TC_MMA_WARP) {
+    // ---- MMA issue: one thread
+    if (lane == 0) {
+      // kind::f16 (bf16 operands, fp32 D), M = 128, N = 3 Cu, A and B MN-major (bits 15, 16)
+      const uint32_t idesc = tc_idesc(128, NCOL) | (1u << 15) | (1u << 16);
+      const uint64_t a0 = tc_smem_desc(smem_u32(ring), 128, WT_ZP * 16);
+      const uint64_t b0 = tc_smem_desc(smem_u32(ring + G::SROWS), 128, WT_ZPU * 16);
+      for (int s = 0; s < my_tiles; ++s) {
+        if (!tc_wait(full + s % NBUF, (uint32_t)((s / NBUF) & 1), abort)) break;
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint64_t boff = (uint64_t)((s % NBUF) * BUF);  // start address in 16-byte units
+#pragma unroll 1
+        for (int t = 0; t < WT_TY; ++t) {
+#pragma unroll
+          for (int xi = 0; xi < WT_TXW; ++xi) {
+            const uint64_t bd = b0 + boff + (uint64_t)(xi * G::XIP + t * KCU * WT_ZPU);
+            const uint32_t accum = (s > 0 || t > 0 || xi > 0) ? 1u : 0u;
+#pragma unroll
+            for (int dz = 0; dz < 3; ++dz) {
+              const uint64_t ad = a0 + boff + (uint64_t)((t * WT_L + xi) * KCS * WT_ZP + dz);
+              asm volatile(
+                  "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem + (uint32_t)(dz * NCOL)),
+                  "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+            }
+          }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+            smem_u32(empty + s % NBUF)));
+      }
+      // `done` completes once every MMA issued above has
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+          smem_u32(done)));
+      volatile int no_abort = 0;
+      tc_wait(done, 0u, &no_abort);
+      if (no_abort) *abort = 1;
+    }
+    __syncwarp();
+  } else {
+    // ---- warps 4-7: bias gradient from each stage, then D -> dw
+    const int g = warp & 3, e = threadIdx.x - 128;
+    constexpr int KB = SWAP ? KCS : KCU;  // 16-byte chunks per output-gradient voxel
+    const int kb = e % KB;                // this thread's chunk (128 is a multiple of KB)
+    float bacc[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) bacc[i] = 0.f;
+    for (int s = 0; s < my_tiles; ++s) {
+      if (!tc_wait(full + s % NBUF, (uint32_t)((s / NBUF) & 1), abort)) break;
+      const uint4* buf = ring + (size_t)(s % NBUF) * BUF;
+      for (int c = e; c < WT_TY * WT_TXW * WT_TZ * KB; c += 128) {
+        const int xi = (c / KB) % WT_TXW, r2 = c / (KB * WT_TXW);
+        const int z = r2 % WT_TZ, t = r2 / WT_TZ;
+        const size_t row = SWAP ? ((size_t)(t * WT_L + xi + 1) * KCS + kb) * WT_ZP + z + 1
+                                : G::SROWS + (size_t)xi * G::XIP + ((t + 1) * KCU + kb) * WT_ZPU + z;
+        const uint4 q = buf[row];
+        const uint32_t w4[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const __nv_bfloat162 b2 = *reinterpret_cast<const __nv_bfloat162*>(&w4[i]);
+          bacc[2 * i] += __low2float(b2);
+          bacc[2 * i + 1] += __high2float(b2);
+        }
+      }
+      __syncwarp();
+      if (lane == 0) tc_arrive(empty + s % NBUF);
+    }
+#pragma unroll
+    for (int off = KB; off < 32; off <<= 1)
+#pragma unroll
+      for (int i = 0; i < 8; ++i) bacc[i] += __shfl_xor_sync(0xffffffffu, bacc[i], off);
+    if (lane < KB) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) atomicAdd(db + kb * 8 + i, bacc[i]);
+    }
+    // D -> dw: warp 4 + g reads TMEM lanes 32 g .. 32 g + 31 = rows (l = g, channel = lane) of S
+    const bool ok = tc_wait(done, 0u, abort);
+    const bool go = __all_sync(0xffffffffu, ok && !*abort) && g < 3 && my_tiles > 0;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (go) {
+#pragma unroll 1
+      for (int dz = 0; dz < 3; ++dz) {
+#pragma unroll 1
+        for (int c16 = 0; c16 < NCOL / 16; ++c16) {
+          uint32_t r[16];
+          const uint32_t taddr = tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)(dz * NCOL + c16 * 16);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+              "[%16];\n"
+              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                "=r"(r[15])
+              : "r"(taddr));
+          asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int n = c16 * 16 + j, lev = n / CU, uc = n % CU;
+            // tap (dy, dz, dx) of S relative to U is (1 - lev, dz - 1, g - 1); mirrored when S is dout
+            const int tap = SWAP ? lev * 9 + (2 - dz) * 3 + (2 - g) : (2 - lev) * 9 + dz * 3 + g;
+            const int co = SWAP ? lane : uc, ci = SWAP ? uc : lane;
+            atomicAdd(dw + ((size_t)tap * COUT + co) * CIN + ci, __uint_as_float(r[j]));
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  if (threadIdx.x == 0 && *abort) atomicExch(err, 1);
+  if (warp == TC_MMA_WARP)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "n"(G::TCOLS));
+}
+
 // ---- launchers ---------------------------------------------------------------
 
 int num_sms() {
@@ -739,6 +992,21 @@ cudaError_t conv_wgrad(const void* in, const void* dout, float* dw, float* db, V
   const int ntiles = v.Y * (v.Z / TZ) * (v.X / TX);
   const int grid = ntiles < num_sms() ? ntiles : num_sms();
   k<<<grid, WG_WARPS * 32, sm, st>>>((const __nv_bfloat16*)in, (const __nv_bfloat16*)dout, dw, db, v);
+  return cudaGetLastError();
+}
+
+template <int CU, bool SWAP>
+cudaError_t conv_wgrad_tc(const void* sop, const void* uop, float* dw, float* db, Vol v, cudaStream_t st) {
+  auto k = k_conv_wgrad_tc<CU, SWAP>;
+  const size_t sm = WtGeom<CU>::smem;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  int* err = nullptr;
+  e = cudaGetSymbolAddress((void**)&err, g_tc_err);
+  if (e != cudaSuccess) return e;
+  const int ntiles = ((v.Y + WT_TY - 1) / WT_TY) * (v.Z / WT_TZ) * (v.X / WT_TXW);
+  const int grid = ntiles < num_sms() ? ntiles : num_sms();
+  k<<<grid, WT_THREADS, sm, st>>>((const __nv_bfloat16*)sop, (const __nv_bfloat16*)uop, dw, db, v, err);
   return cudaGetLastError();
 }
 
@@ -837,6 +1105,28 @@ int lh_sr_conv_wgrad(int32_t cin, int32_t cout, const void* in, const void* dout
   if (cin == 32 && cout == 32) return sr_cuda(lh::sr::conv_wgrad<32, 32>(in, dout, dw, db, v, st));
   if (cin == 32 && cout == 16) return sr_cuda(lh::sr::conv_wgrad<32, 16>(in, dout, dw, db, v, st));
   lh::set_init_error("lh_sr_conv_wgrad: channel pair not built (16->32, 32->32, 32->16)");
+  return LH_EINVAL;
+}
+
+int lh_sr_conv_wgrad_tc(int32_t cin, int32_t cout, const void* in, const void* dout, float* dw, float* db,
+                        int32_t X, int32_t Y, int32_t Z, void* stream) {
+  int rc = sr_check_vol(X, Y, Z);
+  if (rc) return rc;
+  if (Z % lh::sr::WT_TZ) {
+    lh::set_init_error("lh_sr_conv_wgrad_tc: Z must be a multiple of 16");
+    return LH_EINVAL;
+  }
+  if (!in || !dout || !dw || !db || !aligned16(in) || !aligned16(dout)) {
+    lh::set_init_error("lh_sr_conv_wgrad_tc: missing or misaligned pointer");
+    return LH_EINVAL;
+  }
+  const Vol v{X, Y, Z};
+  cudaStream_t st = (cudaStream_t)stream;
+  // the 32-channel operand is the shifted one: the input for 32 -> Cout, the output gradient for 16 -> 32
+  if (cin == 32 && cout == 32) return sr_cuda(lh::sr::conv_wgrad_tc<32, false>(in, dout, dw, db, v, st));
+  if (cin == 32 && cout == 16) return sr_cuda(lh::sr::conv_wgrad_tc<16, false>(in, dout, dw, db, v, st));
+  if (cin == 16 && cout == 32) return sr_cuda(lh::sr::conv_wgrad_tc<16, true>(dout, in, dw, db, v, st));
+  lh::set_init_error("lh_sr_conv_wgrad_tc: channel pair not built (16->32, 32->32, 32->16)");
   return LH_EINVAL;
 }
 

@@ -106,8 +106,9 @@ class SRNet:
         self.flip = [torch.zeros(27 * vw["ci"] * vw["co"], dtype=torch.bfloat16, device=dev) for vw in self.views]
         self.lr, self.betas, self.eps, self.wd = lr, betas, eps, weight_decay
         self.t = 0
-        # forward and data-gradient convolutions on tcgen05 (the default: the warp-specialised TMEM kernel
-        # measures faster than mma.sync in training and inference) or, when unset or Z % 8 != 0, on mma.sync
+        # forward, data-gradient and weight-gradient convolutions on tcgen05 (the default: the warp-specialised
+        # TMEM kernels measure faster than mma.sync) or, when unset or Z is not a multiple of 8 (16 for the
+        # weight gradient), on mma.sync
         self.tcgen05 = tcgen05
         self.sigma = 1.0  # scale of the correction (set by training: rms of the residual it learns)
         self._acts = None
@@ -146,8 +147,9 @@ class SRNet:
         L = load_library()
         vw = self.views[li]
         Y, Z, X = self._shape
-        _check(L.lh_sr_conv_wgrad(vw["ci"], vw["co"], _ptr(x), _ptr(dout), _ptr(vw["gw"]), _ptr(vw["gb"]), X, Y, Z,
-                                  _stream()), "lh_sr_conv_wgrad")
+        fn = L.lh_sr_conv_wgrad_tc if (self.tcgen05 and Z % 16 == 0) else L.lh_sr_conv_wgrad
+        _check(fn(vw["ci"], vw["co"], _ptr(x), _ptr(dout), _ptr(vw["gw"]), _ptr(vw["gb"]), X, Y, Z, _stream()),
+               "lh_sr_conv_wgrad")
 
     def _flip_all(self):
         L = load_library()

@@ -156,6 +156,41 @@ def test_conv_wgrad_and_dgrad(lib, cin, cout):
         np.testing.assert_allclose(dx.float().cpu().numpy(), so.conv_dgrad(d, w), rtol=2 ** -8, atol=1e-3)
 
 
+def test_conv_wgrad_tcgen05_rejects_z_not_multiple_of_16(lib):
+    """Checked before any device work: the tcgen05 weight gradient reduces over 16 z voxels per MMA."""
+    import littleharsh_gb300 as lh
+    assert lib.lh_sr_conv_wgrad_tc(32, 32, None, None, None, None, 32, 5, 8, None) == lh.LH_EINVAL
+    assert b"multiple of 16" in lib.lh_last_error(None)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cin,cout", [(16, 32), (32, 32), (32, 16)])
+@pytest.mark.parametrize("Y,Z,X", [(5, 16, 32), (9, 48, 512)], ids=["12_tiles", "960_tiles"])
+def test_conv_wgrad_tcgen05(lib, cin, cout, Y, Z, X):
+    """The tcgen05 weight and bias gradients against the oracle.  Tiles are 2 levels x 16 z x 8 x columns:
+    an odd Y leaves the second level of the top tiles past the volume (zeros), and 960 tiles give every
+    persistent CTA six or seven, so its ring of stage buffers wraps around.  (16, 32) takes the path with the
+    output gradient as the shifted operand and mirrored taps."""
+    import ctypes
+    import torch
+    from littleharsh_gb300 import srnet
+    rng = np.random.default_rng(900 + cin + cout + Y)
+    x = so.bf16_round(rng.standard_normal((Y, Z, X, cin)))
+    d = so.bf16_round(rng.standard_normal((Y, Z, X, cout)))
+    dw_ref, db_ref = so.conv_wgrad(x, d)
+    dw = torch.zeros((27, cout, cin), dtype=torch.float32, device="cuda")
+    db = torch.zeros(cout, dtype=torch.float32, device="cuda")
+    xt, dt = _t(x, torch.bfloat16), _t(d, torch.bfloat16)
+    assert lib.lh_sr_conv_wgrad_tc(cin, cout, srnet._ptr(xt), srnet._ptr(dt), srnet._ptr(dw), srnet._ptr(db), X, Y,
+                                   Z, None) == 0
+    torch.cuda.synchronize()
+    timed_out = ctypes.c_int32(-1)
+    assert lib.lh_sr_tc_status(ctypes.byref(timed_out)) == 0 and timed_out.value == 0
+    scale = np.abs(dw_ref).max()
+    np.testing.assert_allclose(dw.cpu().numpy(), dw_ref, rtol=1e-4, atol=1e-5 * scale)
+    np.testing.assert_allclose(db.cpu().numpy(), db_ref, rtol=1e-4, atol=1e-4)
+
+
 @pytest.mark.gpu
 def test_mse_and_adam(lib):
     import torch
@@ -195,7 +230,7 @@ def test_network_gradient_matches_oracle(tcgen05):
     import torch
     from littleharsh_gb300 import srnet
     rng = np.random.default_rng(11)
-    Y, Z, X = 4, 8, 32
+    Y, Z, X = 4, 16, 32  # Z a multiple of 16: the weight gradients run on tcgen05 too
     params = srnet.init_params(seed=5)
     # larger second convolutions than the identity-like start and a random tail (it
     # starts at zero) so every path carries gradient
