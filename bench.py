@@ -14,7 +14,8 @@ replicas of all ranks).  A "step" is one full RK3 step (three substages).
 
 With --precision fp64 (the default) the same run also measures the mixed form
 (FP32 transforms, products, nonlinear term and canopy forcing; FP64 solves,
-flow rate and statistics) on the same workload and reports it under "mixed".
+flow rate and statistics) on the same workload and reports it under "mixed",
+and configuration 4's ensemble of 16 uneven replicas (FP64) under "ensemble".
 
 --impl reference times the CPU FP64 restatement of the reference's step (the
 Fortran reference cannot be built here) on all host cores, on a bounded
@@ -290,14 +291,12 @@ def _config(args, cfg: dict, world: int) -> dict:
             if cfg.get("ngalx2") else None}
 
 
-def run_ensemble(args, rank: int, world: int):
+def measure_ensemble(args, prec: int) -> dict:
     """Configuration 4: 16 replicas of uneven sizes advanced together from one graph per step with one stream per
-    replica (the ensemble's default mode, the line's value), beside batched launches (one per kernel kind,
-    substage slot and grid class) and the replicas one by one, each with its own graph; the same start and steps
-    in every mode."""
+    replica (the ensemble's default mode), beside batched launches (one per kernel kind, substage slot and grid
+    class) and the replicas one by one, each with its own graph; the same start and steps in every mode."""
     import littleharsh_gb300 as lh
     cfgs = ensemble_configs()
-    prec = lh.PREC_MIXED if args.precision == "mixed" else lh.PREC_FP64
     members = [build_solver(c, prec, seed=100 + i)[0] for i, c in enumerate(cfgs)]
     pts = sum(m.ngx * m.ngz * m.nyu for m in members)
     start = [m.get_fields() for m in members]
@@ -327,21 +326,32 @@ def run_ensemble(args, rank: int, world: int):
         m.step(args.steps)
         seq += m.last_step_ms()[0]
     b = res["streams"]
-    line = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": b["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if prec == lh.PREC_FP64 else "mixed f32/f64",
-            "data": "synthetic (seeded laminar + 10% perturbation, projected divergence-free)",
-            "config": {"workload": "ensemble16_config4", "replicas": len(members),
-                       "grids": sorted({(m.ngx, m.ngz, m.nyu) for m in members}), "precision": args.precision},
-            "batched": b, "streams": res["streams"],
-            "sequential": {"value": pts * args.steps / (seq / 1e3), "ms_per_step": seq / args.steps,
-                           "launches_per_step": sum(m.last_step_ms()[1] for m in members)},
-            "speedup_vs_sequential": (seq / args.steps) / b["ms_per_step"],
-            "batched_vs_streams": res["streams"]["ms_per_step"] / res["batched"]["ms_per_step"],
-            "gpu_launches": b["launches_per_step"] * args.steps, "clocks": b["clocks"]}
-    print(json.dumps(line), flush=True)
+    out = {"value": b["value"], "unit": UNIT, "ms_per_step": b["ms_per_step"], "mode": "streams",
+           "replicas": len(members), "grids": sorted({(m.ngx, m.ngz, m.nyu) for m in members}),
+           "streams": res["streams"], "batched": res["batched"],
+           "sequential": {"value": pts * args.steps / (seq / 1e3), "ms_per_step": seq / args.steps,
+                          "launches_per_step": sum(m.last_step_ms()[1] for m in members)},
+           "speedup_vs_sequential": (seq / args.steps) / b["ms_per_step"],
+           "batched_vs_streams": res["streams"]["ms_per_step"] / res["batched"]["ms_per_step"],
+           "gpu_launches": b["launches_per_step"] * args.steps, "clocks": b["clocks"]}
     for m in members:
         m.close()
+    return out
+
+
+def run_ensemble(args, rank: int, world: int):
+    import littleharsh_gb300 as lh
+    prec = lh.PREC_MIXED if args.precision == "mixed" else lh.PREC_FP64
+    e = measure_ensemble(args, prec)
+    line = {"metric": METRIC, "value": e["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": e["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if prec == lh.PREC_FP64 else "mixed f32/f64",
+            "data": "synthetic (seeded laminar + 10% perturbation, projected divergence-free)",
+            "config": {"workload": "ensemble16_config4", "replicas": e["replicas"], "grids": e["grids"],
+                       "precision": args.precision},
+            **{k: e[k] for k in ("streams", "batched", "sequential", "speedup_vs_sequential", "batched_vs_streams",
+                                 "gpu_launches", "clocks")}}
+    print(json.dumps(line), flush=True)
 
 
 def _model_per_launch(cfg: dict, s, prof: dict, csz: int) -> dict:
@@ -529,6 +539,13 @@ def run_ours(args, rank: int, world: int, local_rank: int, dist):
                         "launch_shapes": mixed["launch_shapes"],
                         "precision": "FP32 transforms, products, nonlinear term and canopy forcing; FP64 viscous "
                                      "and pressure terms, Helmholtz and pressure solves, flow rate, statistics"}
+    if main_prec == "fp64" and not args.no_ensemble and world == 1 and args.workload == DEFAULT_WORKLOAD:
+        # configuration 4 (16 uneven replicas, FP64) on the same device, the same steps; reported beside the
+        # headline, so a failure there is recorded in the line rather than ending the run
+        try:
+            out["ensemble"] = measure_ensemble(args, lh.PREC_FP64)
+        except Exception as e:  # noqa: BLE001
+            out["ensemble"] = {"error": f"{type(e).__name__}: {e}"}
     if not args.no_cpu_baseline and world == 1:
         try:
             out["cpu_baseline"] = cpu_baseline(cfg, os.cpu_count() or 1)
@@ -550,6 +567,57 @@ def srnet_flops(Y: int, Z: int, X: int, train: bool) -> float:
     return float(f + dgrad + f)
 
 
+def _conv_compare(peaks: dict, args) -> dict:
+    """One 32 -> 32 convolution (bias + ReLU) and one 32 -> 32 weight gradient on configuration 1's volume:
+    mma.sync against tcgen05, CUDA events over 20 launches after warm-up."""
+    import torch
+    import littleharsh_gb300 as lh
+    from littleharsh_gb300 import warmstart as ws
+    from littleharsh_gb300.srnet import _ptr, _stream
+    from littleharsh_gb300.workloads import CONFIG1
+    L = lh.load_library()
+    gi = ws.GridInfo.from_config(CONFIG1)
+    Y, Z, X = gi.nyu, gi.ngz, gi.ngx
+    g = torch.Generator(device="cuda").manual_seed(1)
+    x = torch.randn((Y, Z, X, 32), device="cuda", generator=g).to(torch.bfloat16)
+    d = torch.randn((Y, Z, X, 32), device="cuda", generator=g).to(torch.bfloat16)
+    dw = torch.zeros((27, 32, 32), dtype=torch.float32, device="cuda")
+    db = torch.zeros(32, dtype=torch.float32, device="cuda")
+    w = (torch.randn((27, 32, 32), device="cuda", generator=g) * 0.05).to(torch.bfloat16)
+    bias = torch.zeros(32, dtype=torch.float32, device="cuda")
+    y = torch.empty_like(x)
+    flops = 2.0 * 27 * 32 * 32 * Y * Z * X
+    out = {"volume": [Y, Z, X], "flops": flops}
+    calls = [("wgrad_mma_sync", lambda: L.lh_sr_conv_wgrad(32, 32, _ptr(x), _ptr(d), _ptr(dw), _ptr(db), X, Y, Z,
+                                                          _stream())),
+             ("wgrad_tcgen05", lambda: L.lh_sr_conv_wgrad_tc(32, 32, _ptr(x), _ptr(d), _ptr(dw), _ptr(db), X, Y, Z,
+                                                            _stream())),
+             ("fwd_mma_sync", lambda: L.lh_sr_conv_fwd(32, 32, _ptr(x), _ptr(w), _ptr(bias), _ptr(y), 0, None, None,
+                                                       9, X, Y, Z, _stream())),
+             ("fwd_tcgen05", lambda: L.lh_sr_conv_fwd_tc(32, 32, _ptr(x), _ptr(w), _ptr(bias), _ptr(y), 0, None,
+                                                         None, 9, X, Y, Z, _stream()))]
+    for name, call in calls:
+        if name == "wgrad_tcgen05" and Z % 16:
+            continue
+        for _ in range(max(args.warmup, 3)):
+            if call():
+                raise RuntimeError(f"{name} failed: {L.lh_last_error(None).decode()}")
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n = 20
+        a.record()
+        for _ in range(n):
+            call()
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / n
+        out[f"us_{name}"] = ms * 1e3
+        out[f"tflops_{name}"] = flops / (ms * 1e-3) / 1e12
+        if peaks.get("bf16_tflops"):
+            out[f"frac_of_bf16_peak_{name}"] = out[f"tflops_{name}"] / peaks["bf16_tflops"]
+    return out
+
+
 def run_srnet(args):
     """The super-resolution network's kernels: a training step on configuration 1's
     volume and inference on configuration 5's fine volume, CUDA events around
@@ -562,8 +630,8 @@ def run_srnet(args):
     net = SRNet(seed=0)
     out = {"metric": "SR network bf16 TFLOP/s", "unit": "TFLOP/s", "higher_is_better": True, "n_gpus": 1,
            "dtype": "bf16 (fp32 accumulate)",
-           "kernel": "3x3x3 implicit-GEMM conv on bf16 tensor cores: forward and data gradient on mma.sync m16n8k16 "
-                     "or on tcgen05 (TMEM accumulator), both timed; weight gradient on mma.sync"}
+           "kernel": "3x3x3 implicit-GEMM conv on bf16 tensor cores: forward, data and weight gradients on mma.sync "
+                     "m16n8k16 or on tcgen05 (TMEM accumulators), both timed"}
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
     cases = [("train_step_config1", CONFIG1, True), ("inference_config5_fine", CONFIG5_FINE, False)]
     if args.sr_small:  # profiler captures: the configuration-1 training step only
@@ -602,13 +670,15 @@ def run_srnet(args):
         fl = srnet_flops(Y, Z, X, train)
         best = min(res, key=res.get)  # the faster forward form is the network's default
         tf = fl / (res[best] * 1e-3) / 1e12
-        out[name] = {"volume": [Y, Z, X], "ms": res[best], "tflops": tf, "flops": fl, "forward": "tcgen05" if best else
-                     "mma.sync", "frac_of_bf16_peak": tf / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None,
-                     "ms_mma_sync_forward": res[False], "ms_tcgen05_forward": res[True],
-                     "tflops_tcgen05_forward": fl / (res[True] * 1e-3) / 1e12}
+        out[name] = {"volume": [Y, Z, X], "ms": res[best], "tflops": tf, "flops": fl,
+                     "convolutions": "tcgen05" if best else "mma.sync",
+                     "frac_of_bf16_peak": tf / peaks["bf16_tflops"] if peaks.get("bf16_tflops") else None,
+                     "ms_mma_sync": res[False], "ms_tcgen05": res[True],
+                     "tflops_tcgen05": fl / (res[True] * 1e-3) / 1e12}
         net.tcgen05 = True
         del x, base, tgt
         torch.cuda.empty_cache()
+    out["conv_32x32_config1"] = _conv_compare(peaks, args)
     out["value"] = out["train_step_config1"]["tflops"]
     if "inference_config5_fine" not in out:
         out["note"] = "configuration-1 training step only (--sr-small)"
@@ -679,6 +749,7 @@ def main():
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="with --precision fp64: skip the mixed form's line")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the configuration-4 ensemble in the line")
     ap.add_argument("--ensemble", action="store_true", help="configuration 4: 16 replicas in one graph per step")
     ap.add_argument("--srnet", action="store_true", help="the warm start's network kernels (training and inference)")
     ap.add_argument("--sr-small", action="store_true", help="with --srnet: the configuration-1 training step only")

@@ -374,11 +374,13 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
 // addresses and nothing is copied twice.
 //
 // The CTA is warp-specialised, its roles ordered only by mbarriers:
-//   warps 0-3 (producers) fetch halos with cp.async into a ring of six
-//     buffers; once a thread's copies for a stage have landed it fences them
-//     for the tensor core and arrives on the buffer's `full` barrier (128
-//     arrivals); a buffer is refilled after the `empty` barrier says the MMAs
-//     that read it completed;
+//   warps 0-3 (producers) fetch halos into a ring of six buffers with 16-byte
+//     loads into registers and 16-byte shared stores (cp.async with a zero-fill
+//     size measured slower: its copies were not coalesced, about 32 L2 sectors
+//     and 38 shared wavefronts per warp instruction against 16 and 4); each
+//     thread fences its stores for the tensor core and arrives on the buffer's
+//     `full` barrier (128 arrivals); a buffer is refilled after the `empty`
+//     barrier says the MMAs that read it completed;
 //   warp 8 (one thread) waits on `full`, issues the stage's 9 taps x Cin/16 x 2
 //     tcgen05.mma (K = 16 channels, bf16 operands from shared memory) into the
 //     tile's accumulator set and commits them to `empty` (and, after a tile's
@@ -397,8 +399,6 @@ constexpr int TC_HALO = TC_ZR * TC_XR;       // voxel rows of one k chunk of a h
 constexpr int TC_XP = TC_ZR + 1;             // x pitch in 16-byte rows: odd, so a warp's copies spread over all banks
 constexpr int TC_KP = TC_XR * TC_XP;         // k-chunk pitch in 16-byte rows
 constexpr int TC_NBUF = 6;                   // halo ring (4: 218 us, 6: 203 us, 8: 201 us on 130x96x96)
-constexpr int TC_LAG = 3;                    // stages between issuing a halo's copies and handing it over
-static_assert(TC_LAG >= 1 && TC_LAG <= 4 && TC_LAG < TC_NBUF, "the producer must be able to run TC_LAG stages ahead");
 constexpr int TC_PRODUCERS = 128;            // warps 0-3
 constexpr int TC_THREADS = 288;              // + epilogue warps 4-7 + MMA warp 8
 constexpr int TC_MMA_WARP = 8;
@@ -490,14 +490,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
   if (warp < 4) {
     // ---- producers: stage st = (tile blockIdx.x + (st / 3) gridDim.x, dy = st % 3) into buffer st % NBUF:
-    // rows [k chunk][x + 1][z + 1], x = -1 .. 32, z = -1 .. 8, periodic in x and z, zero outside y
+    // rows [k chunk][x + 1][z + 1], x = -1 .. 32, z = -1 .. 8, periodic in x and z, zero outside y.  16-byte
+    // loads into registers (a warp's loads cover contiguous voxels), then 16-byte shared stores; the buffer is
+    // handed over as soon as its stores are done.
     const int p = threadIdx.x;
-    auto land = [&](int st) {  // this thread's copies of stage st have landed: hand them to the tensor core
-      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-      tc_arrive(full + st % TC_NBUF);
-    };
-    int s = 0;
-    for (; s < nstages; ++s) {
+    constexpr int CH = TC_HALO * KC, PT = (CH + TC_PRODUCERS - 1) / TC_PRODUCERS;
+    for (int s = 0; s < nstages; ++s) {
       if (s >= TC_NBUF && !tc_wait(empty + s % TC_NBUF, (uint32_t)((s / TC_NBUF - 1) & 1), abort)) break;
       const int tile = blockIdx.x + (s / 3) * gridDim.x, dy = s % 3;
       const int xt = tile % ntx, rest = tile / ntx, zt = rest % ntz, y = rest / ntz;
@@ -505,32 +503,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const int gy = y + dy - 1;
       const bool ok = gy >= 0 && gy < v.Y;
       uint4* buf = sA + (size_t)(s % TC_NBUF) * BUF;
-      for (int c = p; c < TC_HALO * KC; c += TC_PRODUCERS) {
-        const int kc = c % KC, u = c / KC;
-        const int xh = u % TC_XR, zz = u / TC_XR;
-        int gz = z0 + zz - 1, gx = x0 + xh - 1;
-        gz = gz < 0 ? gz + v.Z : (gz >= v.Z ? gz - v.Z : gz);
-        gx = gx < 0 ? gx + v.X : (gx >= v.X ? gx - v.X : gx);
-        const size_t vox = ok ? ((size_t)gy * v.Z + gz) * v.X + gx : 0;
-        cp_async16(buf + (size_t)kc * TC_KP + xh * TC_XP + zz, in + vox * CIN + kc * 8, ok);
+      uint4 r[PT];
+      int row[PT];
+#pragma unroll
+      for (int i = 0; i < PT; ++i) {
+        const int c = p + i * TC_PRODUCERS;
+        r[i] = make_uint4(0u, 0u, 0u, 0u);
+        row[i] = -1;
+        if (c < CH) {
+          const int kc = c % KC, u = c / KC;
+          const int xh = u % TC_XR, zz = u / TC_XR;
+          int gz = z0 + zz - 1, gx = x0 + xh - 1;
+          gz = gz < 0 ? gz + v.Z : (gz >= v.Z ? gz - v.Z : gz);
+          gx = gx < 0 ? gx + v.X : (gx >= v.X ? gx - v.X : gx);
+          row[i] = kc * TC_KP + xh * TC_XP + zz;
+          if (ok) r[i] = __ldg(reinterpret_cast<const uint4*>(in + (((size_t)gy * v.Z + gz) * v.X + gx) * CIN + kc * 8));
+        }
       }
-      asm volatile("cp.async.commit_group;\n" ::: "memory");
-      if (s >= TC_LAG) {  // groups of stages <= s - TC_LAG complete: at most TC_LAG pending
-        asm volatile("cp.async.wait_group %0;\n" ::"n"(TC_LAG) : "memory");
-        land(s - TC_LAG);
-      }
+#pragma unroll
+      for (int i = 0; i < PT; ++i)
+        if (row[i] >= 0) buf[row[i]] = r[i];
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      tc_arrive(full + s % TC_NBUF);
     }
-    if (s == nstages) {  // the last TC_LAG stages, oldest first
-      for (int q = nstages - TC_LAG < 0 ? 0 : nstages - TC_LAG; q < nstages; ++q) {
-        const int pending = nstages - 1 - q;
-        if (pending >= 3) asm volatile("cp.async.wait_group 3;\n" ::: "memory");
-        else if (pending == 2) asm volatile("cp.async.wait_group 2;\n" ::: "memory");
-        else if (pending == 1) asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-        else asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        land(q);
-      }
-    }
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   } else if (warp == TC_MMA_WARP) {
     // ---- MMA issue: one thread
     if (lane == 0) {
@@ -691,8 +686,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 //     apart in U's rows [column][level][chunk][z].
 // One MMA per (level of the tile, x column, dz) accumulates D[dz] (128 x 3Cu fp32 in TMEM) over every tile
 // of the persistent CTA; tap (dy, dz, dx) of D[dz][(l, c)][(e, c')] is (1 - e, dz - 1, l - 1) relative to U.
-// Roles as in the forward kernel: warps 0-3 copy a tile's halo into a ring of stage buffers and arrive on
-// `full`; warp 8 (one thread) issues the tile's MMAs and commits them to `empty`; warps 4-7 sum the tile's
+// Roles as in the forward kernel: warps 0-3 copy a tile's halo into a ring of stage buffers (register-staged
+// 16-byte loads and stores) and arrive on `full`; warp 8 (one thread) issues the tile's MMAs and commits them to `empty`; warps 4-7 sum the tile's
 // output gradient (the bias gradient) from the same buffer and arrive on `empty` too, and at the end read
 // D from TMEM and add it to dw.  Every wait is bounded as in the forward kernel.
 constexpr int WT_TXW = 8;               // x columns per tile
@@ -702,7 +697,6 @@ constexpr int WT_L = WT_TXW + 3;        // S halo lines x0 - 1 .. x0 + 9
 constexpr int WT_ZR = WT_TZ + 2;        // S halo z rows
 constexpr int WT_ZP = 19;               // S z pitch in 16-byte rows (odd: a warp's copies spread over all banks)
 constexpr int WT_ZPU = 17;              // U z pitch
-constexpr int WT_LAG = 2;
 constexpr int WT_THREADS = 288;
 
 template <int CU>
@@ -764,54 +758,66 @@ __global__ void __launch_bounds__(WT_THREADS, 1)
   };
 
   if (warp < 4) {
-    // ---- producers: tile s into buffer s % NBUF
+    // ---- producers: tile s into buffer s % NBUF.  16-byte loads into registers, then 16-byte shared stores
+    // (a warp's 32 loads cover 512 contiguous bytes and its stores hit every bank group four times), S first,
+    // then U; the buffer is handed over as soon as its stores are done.
     const int p = threadIdx.x;
-    auto land = [&](int st) {
-      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-      tc_arrive(full + st % NBUF);
-    };
-    int s = 0;
-    for (; s < my_tiles; ++s) {
+    constexpr int SCH = WT_TY * WT_ZR * WT_L * KCS, UCH = G::UL * WT_TZ * WT_TXW * KCU;
+    constexpr int SPT = (SCH + TC_PRODUCERS - 1) / TC_PRODUCERS, UPT = (UCH + TC_PRODUCERS - 1) / TC_PRODUCERS;
+    for (int s = 0; s < my_tiles; ++s) {
       if (s >= NBUF && !tc_wait(empty + s % NBUF, (uint32_t)((s / NBUF - 1) & 1), abort)) break;
       int y0, z0, x0;
       tile_origin(s, y0, z0, x0);
       uint4* buf = ring + (size_t)(s % NBUF) * BUF;
-      // S: rows ((t L + line) 4 + chunk) ZP + zr; levels y0 + t past the top are zeros
-      for (int c = p; c < WT_TY * WT_ZR * WT_L * KCS; c += TC_PRODUCERS) {
-        const int kc = c % KCS, line = (c / KCS) % WT_L, r2 = c / (KCS * WT_L);
-        const int zr = r2 % WT_ZR, t = r2 / WT_ZR;
-        const int gy = y0 + t;
-        const bool ok = gy < v.Y;
-        int gz = z0 + zr - 1, gx = x0 + line - 1;
-        gz = gz < 0 ? gz + v.Z : (gz >= v.Z ? gz - v.Z : gz);
-        gx = gx < 0 ? gx + v.X : (gx >= v.X ? gx - v.X : gx);
-        const size_t vox = ok ? ((size_t)gy * v.Z + gz) * v.X + gx : 0;
-        cp_async16(buf + ((size_t)(t * WT_L + line) * KCS + kc) * WT_ZP + zr, sop + vox * 32 + kc * 8, ok);
+      {  // S: rows ((t L + line) 4 + chunk) ZP + zr; levels y0 + t past the top are zeros
+        uint4 r[SPT];
+        int row[SPT];
+#pragma unroll
+        for (int i = 0; i < SPT; ++i) {
+          const int c = p + i * TC_PRODUCERS;
+          r[i] = make_uint4(0u, 0u, 0u, 0u);
+          row[i] = -1;
+          if (c < SCH) {
+            const int kc = c % KCS, line = (c / KCS) % WT_L, r2 = c / (KCS * WT_L);
+            const int zr = r2 % WT_ZR, t = r2 / WT_ZR;
+            const int gy = y0 + t;
+            int gz = z0 + zr - 1, gx = x0 + line - 1;
+            gz = gz < 0 ? gz + v.Z : (gz >= v.Z ? gz - v.Z : gz);
+            gx = gx < 0 ? gx + v.X : (gx >= v.X ? gx - v.X : gx);
+            row[i] = ((t * WT_L + line) * KCS + kc) * WT_ZP + zr;
+            if (gy < v.Y)
+              r[i] = __ldg(reinterpret_cast<const uint4*>(sop + (((size_t)gy * v.Z + gz) * v.X + gx) * 32 + kc * 8));
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < SPT; ++i)
+          if (row[i] >= 0) buf[row[i]] = r[i];
       }
-      // U: rows SROWS + column XIP + (level KCU + chunk) ZPU + z; levels y0 - 1 .. y0 + 2, zeros outside
-      for (int c = p; c < G::UL * WT_TZ * WT_TXW * KCU; c += TC_PRODUCERS) {
-        const int kcu = c % KCU, xi = (c / KCU) % WT_TXW, r2 = c / (KCU * WT_TXW);
-        const int z = r2 % WT_TZ, lev = r2 / WT_TZ;
-        const int gy = y0 + lev - 1;
-        const bool ok = gy >= 0 && gy < v.Y;
-        const size_t vox = ok ? ((size_t)gy * v.Z + z0 + z) * v.X + x0 + xi : 0;
-        cp_async16(buf + G::SROWS + (size_t)xi * G::XIP + (lev * KCU + kcu) * WT_ZPU + z, uop + vox * CU + kcu * 8,
-                   ok);
+      {  // U: rows SROWS + column XIP + (level KCU + chunk) ZPU + z; levels y0 - 1 .. y0 + 2, zeros outside
+        uint4 r[UPT];
+        int row[UPT];
+#pragma unroll
+        for (int i = 0; i < UPT; ++i) {
+          const int c = p + i * TC_PRODUCERS;
+          r[i] = make_uint4(0u, 0u, 0u, 0u);
+          row[i] = -1;
+          if (c < UCH) {
+            const int kcu = c % KCU, xi = (c / KCU) % WT_TXW, r2 = c / (KCU * WT_TXW);
+            const int z = r2 % WT_TZ, lev = r2 / WT_TZ;
+            const int gy = y0 + lev - 1;
+            row[i] = G::SROWS + xi * G::XIP + (lev * KCU + kcu) * WT_ZPU + z;
+            if (gy >= 0 && gy < v.Y)
+              r[i] = __ldg(reinterpret_cast<const uint4*>(uop + (((size_t)gy * v.Z + z0 + z) * v.X + x0 + xi) * CU +
+                                                          kcu * 8));
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < UPT; ++i)
+          if (row[i] >= 0) buf[row[i]] = r[i];
       }
-      asm volatile("cp.async.commit_group;\n" ::: "memory");
-      if (s >= WT_LAG) {
-        asm volatile("cp.async.wait_group %0;\n" ::"n"(WT_LAG) : "memory");
-        land(s - WT_LAG);
-      }
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+      tc_arrive(full + s % NBUF);
     }
-    if (s == my_tiles) {
-      for (int q = my_tiles - WT_LAG < 0 ? 0 : my_tiles - WT_LAG; q < my_tiles; ++q) {
-        if (my_tiles - 1 - q >= 1) asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-        else asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        land(q);
-      }
-    }
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   } else if (warp == TC_MMA_WARP) {
     // ---- MMA issue: one thread
     if (lane == 0) {
