@@ -820,6 +820,13 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
       return bail(rc);
     h->t.kx = pkx; h->t.kz = pkz; h->t.k2x = pk2x; h->t.k2z = pk2z; h->t.d2u = pd2u; h->t.d2v = pd2v;
     h->t.cu = pcu; h->t.cv = pcv; h->t.wc = pwc; h->t.wf = pwf; h->t.dyc = pdyc; h->t.dyvw = pdyvw;
+    // the same values rounded to float (to nearest, as a device conversion would round them)
+    auto rounded = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
+    float *pkxf, *pkzf, *pcuf, *pcvf;
+    if ((rc = upload(h, &pkxf, rounded(h->kx))) || (rc = upload(h, &pkzf, rounded(h->kz))) ||
+        (rc = upload(h, &pcuf, rounded(cu))) || (rc = upload(h, &pcvf, rounded(cv))))
+      return bail(rc);
+    h->t.kxf = pkxf; h->t.kzf = pkzf; h->t.cuf = pcuf; h->t.cvf = pcvf;
   }
   // pressure LU per column (LU_buildP + LU_decP)
   {

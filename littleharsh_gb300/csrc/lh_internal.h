@@ -86,6 +86,12 @@ struct Tables {
   const double* dg1;   // [nyp] pressure LU lower diagonal (column independent)
   const double* dg2;   // [nyp][np] pressure LU 1/diag per column
   const double* dg3;   // [nyp][np] pressure LU scaled upper diagonal per column
+  // kx, kz, cu, cv rounded to FP32 once (the mixed form's nonlinear term combines its FP32 spectra with them;
+  // on this part a conversion costs about as much as an FP64 instruction)
+  const float* kxf;
+  const float* kzf;
+  const float* cuf;
+  const float* cvf;
 };
 
 // Canopy forcing: processed planes of one field.

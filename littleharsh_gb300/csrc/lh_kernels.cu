@@ -519,10 +519,14 @@ template <> __device__ __forceinline__ const float2* prod<float2>(const AsmArgs&
 __device__ __forceinline__ double2 nterm(double2 A, double2 B, double2 D1, double2 D0, double kx, double kz, double c) {
   return double2{(-kx * A.y - kz * B.y) + c * (D1.x - D0.x), (kx * A.x + kz * B.x) + c * (D1.y - D0.y)};
 }
-__device__ __forceinline__ double2 nterm(float2 A, float2 B, float2 D1, float2 D0, double kx, double kz, double c) {
-  const float fx = (float)kx, fz = (float)kz, fc = (float)c;
+__device__ __forceinline__ double2 nterm(float2 A, float2 B, float2 D1, float2 D0, float fx, float fz, float fc) {
   return double2{(double)((-fx * A.y - fz * B.y) + fc * (D1.x - D0.x)),
                  (double)((fx * A.x + fz * B.x) + fc * (D1.y - D0.y))};
+}
+// the wavenumbers and the y metric in the precision the product spectra are combined in
+template <typename P> __device__ __forceinline__ auto wnum(const double* d, const float* f, int i) {
+  if constexpr (sizeof(P) == sizeof(float2)) return __ldg(f + i);
+  else return d[i];
 }
 
 template <typename P>
@@ -550,7 +554,6 @@ __device__ __forceinline__ void assemble_body(const AsmArgs& a, const Dims& d, c
   } else {
     const double a1 = t.d2u[3 * jj], a2 = t.d2u[3 * jj + 1], a3 = t.d2u[3 * jj + 2];
     const double2 pc = ld(a.p + (size_t)(jj - 1) * np + col);
-    const double c = t.cu[jj];
     const size_t f1 = (size_t)jj * np + col, f0 = f1 - np;  // faces jj and jj-1
     const bool tip = (jj == a.tipu[0] || jj == a.tipu[1]);
     const int tslot = (jj == a.tipu[0]) ? 0 : 1;
@@ -573,7 +576,7 @@ __device__ __forceinline__ void assemble_body(const AsmArgs& a, const Dims& d, c
       // a short column's product is zero on the middle band's planes (they hold only long modes)
       const P D1 = (lng || !coarse_v(d, jj)) ? ld(D + f1) : P{0, 0};
       const P D0 = (lng || !coarse_v(d, jj - 1)) ? ld(D + f0) : P{0, 0};
-      const double2 N = nterm(A, B, D1, D0, kx, kz, c);
+      const double2 N = nterm(A, B, D1, D0, wnum<P>(t.kx, t.kxf, i), wnum<P>(t.kz, t.kzf, kk), wnum<P>(t.cu, t.cuf, jj));
       const double nr = N.x, ni = N.y;
       (f == 0 ? a.n1 : a.n3)[c0] = double2{nr, ni};
       rx = rx - a.g * nr;
@@ -604,8 +607,7 @@ __device__ __forceinline__ void assemble_body(const AsmArgs& a, const Dims& d, c
       double ry = a.C1 * L_y + a.C2 * nold.y + C3 * (p1.y - p0.y);
       const P A = ld(prod<P>(a, 4) + c0), B = ld(prod<P>(a, 5) + c0);
       const P V1 = ld(prod<P>(a, 3) + c0 + np), V0 = ld(prod<P>(a, 3) + c0);
-      const double c = t.cv[jj];
-      const double2 N = nterm(A, B, V1, V0, kx, kz, c);
+      const double2 N = nterm(A, B, V1, V0, wnum<P>(t.kx, t.kxf, i), wnum<P>(t.kz, t.kzf, kk), wnum<P>(t.cv, t.cvf, jj));
       const double nr = N.x, ni = N.y;
       a.n2[c0] = double2{nr, ni};
       rx = rx - a.g * nr;
