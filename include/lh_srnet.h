@@ -42,10 +42,10 @@ int lh_sr_conv_fwd(int32_t cin, int32_t cout, const void* in, const void* w, con
                    void* stream);
 
 /* The same convolution on the tcgen05 tensor cores (TMEM accumulators, one
- * elected thread issuing the MMAs, staging of the next y offset overlapped
- * with the MMAs of the current one through two buffers and their mbarriers);
- * Z must also be a multiple of 8.  If an MMA completion wait runs out, the
- * CTA stops and records it for lh_sr_tc_status. */
+ * elected thread issuing the MMAs, producer warps staging the halos of the
+ * next y offsets into a ring of buffers while the MMAs read the current one,
+ * ordered by mbarriers); Z must also be a multiple of 8.  If an mbarrier wait
+ * runs out, the CTA stops and records it for lh_sr_tc_status. */
 int lh_sr_conv_fwd_tc(int32_t cin, int32_t cout, const void* in, const void* w, const float* bias, void* out,
                       int32_t out_f32, const void* res, const void* gate, int32_t flags, int32_t X, int32_t Y,
                       int32_t Z, void* stream);

@@ -22,6 +22,8 @@
 //   weight gradient: rows = output channels, columns = input channels,
 //     reduction = voxels, one warp per 3 taps, accumulated in registers over
 //     all tiles of the persistent CTA and added to the fp32 gradient once.
+// The tcgen05 forms of the forward convolution and the weight gradient follow
+// the mma.sync kernels below; the network uses them by default.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
