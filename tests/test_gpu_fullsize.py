@@ -1,7 +1,8 @@
 """Configuration 2 at full size (576 x 576 points, 450 u levels, 48 x 24 posts; ~19 GB per solver).
 
 Against the oracle on the same projected seeded field: two FP64 RK3 steps within 1e-10 relative L2 on u, v, w
-and p, the mixed form within 1e-4 (the oracle takes a few seconds per step on the host's cores at this size).
+and p, the mixed form within 1e-4 (the oracle takes a few seconds per step on the host's cores at this size);
+the same for one step on the warm start's fine grid (configuration 5: 576 x 576 points, 385 levels).
 Besides, properties that do not depend on the size hold after a few RK3 steps:
 
 * the projection leaves the field divergence free (max |div| at round-off);
@@ -138,6 +139,33 @@ def test_configuration2_against_the_oracle(oracle_mod):
         s.set_fields(u1, u2, u3, p)
         s.set_time(0.0, dt, 0.0, Q)
         s.step(2)
+        for name, a, b in zip(("u1", "u2", "u3", "p"), s.get_fields(), ref):
+            e = rel_l2(a, b)
+            assert e < tol, f"precision {prec} {name}: rel L2 {e:.3e} >= {tol:.0e}"
+        assert abs(s.time()["mpgx"] - mpgx) < (1e-9 if prec == lh.PREC_FP64 else 1e-4) * abs(mpgx)
+        s.close()
+
+
+def test_configuration5_fine_grid_against_the_oracle(oracle_mod):
+    """The warm start's fine grid (576 x 576 points, 385 levels, Re_b 2800, 12 x 6 posts 12 x 24 points wide,
+    64-level canopies) stepped once by the GPU (FP64 and mixed) and by the oracle from one projected field."""
+    import littleharsh_gb300 as lh
+    from littleharsh_gb300.workloads import CONFIG5_FINE
+    from tests.helpers import projected_ic
+    o = oracle_mod.Oracle(**CONFIG5_FINE)
+    u1, u2, u3, p = projected_ic(o, seed=9)
+    dt, Q = o.cfl_dt(0.5), o.flowrate()
+    o.set_fields(u1, u2, u3, p)
+    o.set_scalars(0.0, dt, 0.0, Q)
+    o.step(1)
+    ref = o.get_fields()
+    mpgx = o.scalars()["mpgx"]
+    del o
+    for prec, tol in ((lh.PREC_FP64, 1e-10), (lh.PREC_MIXED, 1e-4)):
+        s = lh.Solver(lh.Config(**CONFIG5_FINE), precision=prec)
+        s.set_fields(u1, u2, u3, p)
+        s.set_time(0.0, dt, 0.0, Q)
+        s.step(1)
         for name, a, b in zip(("u1", "u2", "u3", "p"), s.get_fields(), ref):
             e = rel_l2(a, b)
             assert e < tol, f"precision {prec} {name}: rel L2 {e:.3e} >= {tol:.0e}"
