@@ -81,6 +81,7 @@ struct lh_handle {
   Dims dmid{};              // the middle band's plane geometry (bands only)
   int tx = 8, chunk = 16;
   int xsplit = 0;  // x-pass: face pair transformed on its own (smaller shared-memory footprint)
+  int xthreads = 256;  // x-pass: threads per CTA (128 or 256)
   // state
   double t_now = 0, dt = 0;
   bool have_fields = false, have_dt = false;
@@ -388,7 +389,7 @@ int nl_bands(const lh_handle* h, NlBand<R>* out) {
       for (int i = 0; i < 6; ++i) a.out[i] = (T2*)h->mixp[i];
       a.wc = h->t.wc; a.wf = h->t.wf; a.dyc = h->t.dyc;
       a.dxi = db.ngx / h->Lx; a.dzi = db.ngz / h->Lz;
-      a.sc = h->sc; a.want_cfl = 0; a.chunk = h->chunk; a.split = h->xsplit;
+      a.sc = h->sc; a.want_cfl = 0; a.chunk = h->chunk; a.split = h->xsplit; a.threads = h->xthreads;
       a.c_lo = B.c_lo; a.c_hi = B.c_hi; a.f_lo = B.f_lo; a.f_hi = B.f_hi;
       a.mean_split = sizeof(R) == 4;
       a.us = h->u1; a.ws = h->u3; a.nps = d.np;
@@ -966,6 +967,7 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
   if (const char* v = std::getenv("LH_TX")) { const int x = std::atoi(v); if (x >= 1 && x <= 64) h->tx = x; }
   if (const char* v = std::getenv("LH_CHUNK")) { const int x = std::atoi(v); if (x >= 1 && x <= 4096) h->chunk = x; }
   if (const char* v = std::getenv("LH_XSPLIT")) h->xsplit = std::atoi(v) != 0 ? 1 : 0;
+  if (const char* v = std::getenv("LH_XTHREADS")) h->xthreads = std::atoi(v) == 128 ? 128 : 256;
   {
     const cudaError_t e = configure_kernels();
     if (e != cudaSuccess) return bail(fail(h, LH_ECUDA, "kernel attributes: %s", cudaGetErrorString(e)));
@@ -1627,6 +1629,21 @@ int lh_autotune(lh_handle* h, int32_t* tx_out, int32_t* chunk_out) {
     h->xsplit = t2[1] < t2[0] ? 1 : 0;
     if (h->xsplit != xs0 && h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; ++h->graph_gen; }
   }
+  // threads per x-pass CTA: the transforms' stages have 100-200 butterflies, so 128 threads with twice the
+  // CTAs per SM can beat 256
+  {
+    const int xt0 = h->xthreads;
+    float t2[2] = {0.f, 0.f};
+    const int cand[2] = {256, 128};
+    for (int c = 0; c < 2; ++c) {
+      h->xthreads = cand[c];
+      t2[c] = h->precision == LH_PREC_MIXED ? time_parts<float>(h, false, true, e0, e1)
+                                            : time_parts<double>(h, false, true, e0, e1);
+      if (t2[c] < 0.f) { h->xthreads = xt0; cudaEventDestroy(e0); cudaEventDestroy(e1); return fail(h, LH_ECUDA, "autotune: product pass failed"); }
+    }
+    h->xthreads = t2[1] < t2[0] ? 128 : 256;
+    if (h->xthreads != xt0 && h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; ++h->graph_gen; }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   CU(h, cudaGetLastError());
@@ -1644,6 +1661,12 @@ int lh_get_launch_shapes(lh_handle* h, int32_t* tx, int32_t* chunk, int32_t* xsp
   if (tx) *tx = h->tx;
   if (chunk) *chunk = h->chunk;
   if (xsplit) *xsplit = h->xsplit;
+  return LH_OK;
+}
+
+int lh_get_x_threads(lh_handle* h, int32_t* threads) {
+  if (!h || !threads) return LH_EINVAL;
+  *threads = h->xthreads;
   return LH_OK;
 }
 
@@ -1713,7 +1736,7 @@ int lh_cfl_dt(lh_handle* h, double cfl, double* dt_out) {
       for (int i = 0; i < 6; ++i) a.out[i] = (T2*)h->mixp[i];
       a.wc = h->t.wc; a.wf = h->t.wf; a.dyc = h->t.dyc;
       a.dxi = db.ngx / h->Lx; a.dzi = db.ngz / h->Lz;
-      a.sc = h->sc; a.want_cfl = 1; a.chunk = h->chunk; a.split = h->xsplit;
+      a.sc = h->sc; a.want_cfl = 1; a.chunk = h->chunk; a.split = h->xsplit; a.threads = h->xthreads;
       a.c_lo = B.c_lo; a.c_hi = B.c_hi; a.f_lo = B.c_lo; a.f_hi = B.c_lo - 1;  // centres only
       launch_xprod<R>(a, db, *B.ph, *B.pf, B.rtw, h->st);
     }

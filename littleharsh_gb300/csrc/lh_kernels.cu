@@ -428,7 +428,7 @@ void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const 
   size_t sm;
   xprod_shape(a, d, &grid, &sm);
   if (grid.x == 0) return;
-  k_xprod<R><<<grid, 256, sm, st>>>(a, d, ph, pf, rtw);
+  k_xprod<R><<<grid, a.threads == 128 ? 128 : 256, sm, st>>>(a, d, ph, pf, rtw);
 }
 
 // Canopy forcing on one mixed row of one processed plane: x-inverse, solid

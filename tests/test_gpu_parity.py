@@ -172,6 +172,7 @@ def test_autotune_keeps_results(oracle_mod):
     t.set_time(0.0, tm["dt"], 0.0, tm["QxT"])
     shapes = t.autotune()
     assert shapes["tx"] in (1, 2, 4, 8, 16, 32) and shapes["chunk"] in (4, 8, 16, 32, 64)
+    assert shapes["xthreads"] in (128, 256)
     s.step(3)
     t.step(3)
     for a, b in zip(t.get_fields(), s.get_fields()):
@@ -189,6 +190,27 @@ def test_split_face_pair_keeps_results(oracle_mod, monkeypatch, mixed):
     for split in ("0", "1"):
         monkeypatch.setenv("LH_XSPLIT", split)
         s = lh.Solver(lh.Config(**C1), precision=prec)
+        s.set_fields(*s0.get_fields())
+        tm = s0.time()
+        s.set_time(0.0, tm["dt"], 0.0, tm["QxT"])
+        s.step(3)
+        sols.append(s)
+    for a, b in zip(sols[0].get_fields(), sols[1].get_fields()):
+        np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_x_pass_threads_keep_results(oracle_mod, monkeypatch, mixed):
+    """128 or 256 threads per product-pass CTA share the same butterflies out differently, not the
+    arithmetic: bit for bit the same step."""
+    import littleharsh_gb300 as lh
+    o, s0 = _pair(oracle_mod, C1)
+    prec = lh.PREC_MIXED if mixed else lh.PREC_FP64
+    sols = []
+    for threads in ("256", "128"):
+        monkeypatch.setenv("LH_XTHREADS", threads)
+        s = lh.Solver(lh.Config(**C1), precision=prec)
+        assert s.launch_shapes()["xthreads"] == int(threads)
         s.set_fields(*s0.get_fields())
         tm = s0.time()
         s.set_time(0.0, tm["dt"], 0.0, tm["QxT"])
