@@ -252,8 +252,9 @@ int lh_profile_step(lh_handle* h, double* ms_by_kind, int32_t* count_by_kind, in
 /* Launch-shape autotuner (no reference counterpart).  Times the z passes for
  * each z tile width (columns per CTA) and the product pass for each number of
  * levels per CTA on this handle's grid and precision, keeps the fastest of
- * each, then the product pass's buffer split and threads per CTA (read them
- * back with lh_get_launch_shapes and lh_get_x_threads), keeps the fastest of
+ * each, the z passes' and the product pass's threads per CTA and the product
+ * pass's buffer split (read them back with lh_get_launch_shapes,
+ * lh_get_z_threads and lh_get_x_threads), keeps the fastest of
  * each and returns the first two (either pointer may be NULL).  Needs fields; writes
  * only scratch, so the fields and the time are unchanged.  The next step is
  * captured with the new shapes. */
@@ -270,6 +271,12 @@ int lh_get_launch_shapes(lh_handle* h, int32_t* tx, int32_t* chunk, int32_t* xsp
  * counterpart); lh_autotune picks it by timing.  Batched ensemble launches
  * always use 256. */
 int lh_get_x_threads(lh_handle* h, int32_t* threads);
+
+/* Threads per CTA of the z passes (nonlinear term and canopy forcing) the
+ * next step uses (128 or 256; no reference counterpart); lh_autotune picks it
+ * by timing at the z tile width it chose.  Batched ensemble launches always
+ * use 256. */
+int lh_get_z_threads(lh_handle* h, int32_t* threads);
 
 
 /* Divergence-free projection (solveP + v_corr with kRK = 1, the operation of

@@ -82,6 +82,7 @@ struct lh_handle {
   int tx = 8, chunk = 16;
   int xsplit = 0;  // x-pass: face pair transformed on its own (smaller shared-memory footprint)
   int xthreads = 256;  // x-pass: threads per CTA (128 or 256)
+  int zthreads = 256;  // z passes of the nonlinear term and the canopy forcing: threads per CTA (128 or 256)
   // state
   double t_now = 0, dt = 0;
   bool have_fields = false, have_dt = false;
@@ -421,7 +422,7 @@ void enqueue_nonlinear(lh_handle* h, cudaStream_t st, bool zinv, bool xprod, boo
   for (int b = 0; b < nbl; ++b) {
     const NlBand<R>& B = bl[b];
     if (zinv) {
-      launch_zinv<R>(B.zi, *B.d, *B.pz, h->tx, st);
+      launch_zinv<R>(B.zi, *B.d, *B.pz, h->tx, st, h->zthreads);
       mark(h, K_ZINV);
     }
     if (xprod) {
@@ -429,7 +430,7 @@ void enqueue_nonlinear(lh_handle* h, cudaStream_t st, bool zinv, bool xprod, boo
       mark(h, K_XPROD);
     }
     if (zfwd) {
-      launch_zfwd<R>(B.zf, *B.d, *B.pz, h->tx, 1.0 / B.d->ngz, st);
+      launch_zfwd<R>(B.zf, *B.d, *B.pz, h->tx, 1.0 / B.d->ngz, st, h->zthreads);
       mark(h, K_ZFWD);
     }
   }
@@ -527,11 +528,11 @@ int enqueue_substage(lh_handle* h, int k, int upto) {
     ZJobs<R> zi, zf;
     MaskArgs<R> m;
     if (ib_args<R>(h, k, &zi, &m, &zf)) {
-      launch_zinv<R>(zi, d, h->pz.plan, h->tx, st);
+      launch_zinv<R>(zi, d, h->pz.plan, h->tx, st, h->zthreads);
       mark(h, K_IB_ZINV);
       launch_xmask<R>(m, d, h->ph.plan, h->rtw, st);
       mark(h, K_IB_XMASK);
-      launch_zfwd<R>(zf, d, h->pz.plan, h->tx, 1.0 / d.ngz, st);
+      launch_zfwd<R>(zf, d, h->pz.plan, h->tx, 1.0 / d.ngz, st, h->zthreads);
       mark(h, K_IB_ZFWD);
     }
   }
@@ -968,6 +969,7 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
   if (const char* v = std::getenv("LH_CHUNK")) { const int x = std::atoi(v); if (x >= 1 && x <= 4096) h->chunk = x; }
   if (const char* v = std::getenv("LH_XSPLIT")) h->xsplit = std::atoi(v) != 0 ? 1 : 0;
   if (const char* v = std::getenv("LH_XTHREADS")) h->xthreads = std::atoi(v) == 128 ? 128 : 256;
+  if (const char* v = std::getenv("LH_ZTHREADS")) h->zthreads = std::atoi(v) == 128 ? 128 : 256;
   {
     const cudaError_t e = configure_kernels();
     if (e != cudaSuccess) return bail(fail(h, LH_ECUDA, "kernel attributes: %s", cudaGetErrorString(e)));
@@ -1607,6 +1609,20 @@ int lh_autotune(lh_handle* h, int32_t* tx_out, int32_t* chunk_out) {
     if (ms < best) { best = ms; best_tx = tx; }
   }
   h->tx = best_tx;
+  // threads per z-pass CTA at that width
+  {
+    const int zt0 = h->zthreads;
+    float t2[2] = {0.f, 0.f};
+    const int cand[2] = {256, 128};
+    for (int c = 0; c < 2; ++c) {
+      h->zthreads = cand[c];
+      t2[c] = h->precision == LH_PREC_MIXED ? time_parts<float>(h, true, false, e0, e1)
+                                            : time_parts<double>(h, true, false, e0, e1);
+      if (t2[c] < 0.f) { h->zthreads = zt0; cudaEventDestroy(e0); cudaEventDestroy(e1); return fail(h, LH_ECUDA, "autotune: z passes failed"); }
+    }
+    h->zthreads = t2[1] < t2[0] ? 128 : 256;
+    if (h->zthreads != zt0 && h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; ++h->graph_gen; }
+  }
   best = 1e30f;
   for (int ch : {4, 8, 16, 32, 64}) {
     h->chunk = ch;
@@ -1667,6 +1683,12 @@ int lh_get_launch_shapes(lh_handle* h, int32_t* tx, int32_t* chunk, int32_t* xsp
 int lh_get_x_threads(lh_handle* h, int32_t* threads) {
   if (!h || !threads) return LH_EINVAL;
   *threads = h->xthreads;
+  return LH_OK;
+}
+
+int lh_get_z_threads(lh_handle* h, int32_t* threads) {
+  if (!h || !threads) return LH_EINVAL;
+  *threads = h->zthreads;
   return LH_OK;
 }
 

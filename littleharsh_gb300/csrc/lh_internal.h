@@ -134,9 +134,10 @@ struct ZJobs {
 
 // Launchers (lh_kernels.cu).  All are asynchronous on `st`.
 template <typename R>
-void launch_zinv(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, cudaStream_t st);
+void launch_zinv(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, cudaStream_t st, int threads = 256);
 template <typename R>
-void launch_zfwd(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, double scale, cudaStream_t st);
+void launch_zfwd(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, double scale, cudaStream_t st,
+                 int threads = 256);
 
 template <typename R>
 struct ProdArgs {

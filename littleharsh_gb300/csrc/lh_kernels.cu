@@ -141,21 +141,22 @@ void zpass_shape(const ZJobs<R>& jobs, const Dims& d, int tx, dim3* grid, size_t
 }
 
 template <typename R>
-void launch_zinv(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, cudaStream_t st) {
+void launch_zinv(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, cudaStream_t st, int threads) {
   dim3 grid;
   size_t sm;
   zpass_shape(jobs, d, tx, &grid, &sm);
   if (grid.x == 0) return;
-  k_zinv<R><<<grid, 256, sm, st>>>(jobs, d, pz, tx);
+  k_zinv<R><<<grid, threads == 128 ? 128 : 256, sm, st>>>(jobs, d, pz, tx);
 }
 
 template <typename R>
-void launch_zfwd(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, double scale, cudaStream_t st) {
+void launch_zfwd(const ZJobs<R>& jobs, const Dims& d, const FftPlan& pz, int tx, double scale, cudaStream_t st,
+                 int threads) {
   dim3 grid;
   size_t sm;
   zpass_shape(jobs, d, tx, &grid, &sm);
   if (grid.x == 0) return;
-  k_zfwd<R><<<grid, 256, sm, st>>>(jobs, d, pz, tx, scale);
+  k_zfwd<R><<<grid, threads == 128 ? 128 : 256, sm, st>>>(jobs, d, pz, tx, scale);
 }
 
 // ---------------------------------------------------------------------------
@@ -1450,10 +1451,10 @@ cudaError_t configure_kernels() {
   return cudaSuccess;
 }
 
-template void launch_zinv<double>(const ZJobs<double>&, const Dims&, const FftPlan&, int, cudaStream_t);
-template void launch_zinv<float>(const ZJobs<float>&, const Dims&, const FftPlan&, int, cudaStream_t);
-template void launch_zfwd<double>(const ZJobs<double>&, const Dims&, const FftPlan&, int, double, cudaStream_t);
-template void launch_zfwd<float>(const ZJobs<float>&, const Dims&, const FftPlan&, int, double, cudaStream_t);
+template void launch_zinv<double>(const ZJobs<double>&, const Dims&, const FftPlan&, int, cudaStream_t, int);
+template void launch_zinv<float>(const ZJobs<float>&, const Dims&, const FftPlan&, int, cudaStream_t, int);
+template void launch_zfwd<double>(const ZJobs<double>&, const Dims&, const FftPlan&, int, double, cudaStream_t, int);
+template void launch_zfwd<float>(const ZJobs<float>&, const Dims&, const FftPlan&, int, double, cudaStream_t, int);
 template void launch_xprod<double>(const ProdArgs<double>&, const Dims&, const FftPlan&, const FftPlan&, const double2*,
                                    cudaStream_t);
 template void launch_xprod<float>(const ProdArgs<float>&, const Dims&, const FftPlan&, const FftPlan&, const double2*,

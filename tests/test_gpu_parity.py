@@ -172,7 +172,7 @@ def test_autotune_keeps_results(oracle_mod):
     t.set_time(0.0, tm["dt"], 0.0, tm["QxT"])
     shapes = t.autotune()
     assert shapes["tx"] in (1, 2, 4, 8, 16, 32) and shapes["chunk"] in (4, 8, 16, 32, 64)
-    assert shapes["xthreads"] in (128, 256)
+    assert shapes["xthreads"] in (128, 256) and shapes["zthreads"] in (128, 256)
     s.step(3)
     t.step(3)
     for a, b in zip(t.get_fields(), s.get_fields()):
@@ -200,17 +200,18 @@ def test_split_face_pair_keeps_results(oracle_mod, monkeypatch, mixed):
 
 
 @pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
-def test_x_pass_threads_keep_results(oracle_mod, monkeypatch, mixed):
-    """128 or 256 threads per product-pass CTA share the same butterflies out differently, not the
-    arithmetic: bit for bit the same step."""
+@pytest.mark.parametrize("which", ["x", "z"])
+def test_pass_threads_keep_results(oracle_mod, monkeypatch, mixed, which):
+    """128 or 256 threads per product-pass (x) or z-pass CTA share the same butterflies out differently,
+    not the arithmetic: bit for bit the same step."""
     import littleharsh_gb300 as lh
     o, s0 = _pair(oracle_mod, C1)
     prec = lh.PREC_MIXED if mixed else lh.PREC_FP64
     sols = []
     for threads in ("256", "128"):
-        monkeypatch.setenv("LH_XTHREADS", threads)
+        monkeypatch.setenv(f"LH_{which.upper()}THREADS", threads)
         s = lh.Solver(lh.Config(**C1), precision=prec)
-        assert s.launch_shapes()["xthreads"] == int(threads)
+        assert s.launch_shapes()[f"{which}threads"] == int(threads)
         s.set_fields(*s0.get_fields())
         tm = s0.time()
         s.set_time(0.0, tm["dt"], 0.0, tm["QxT"])
