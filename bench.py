@@ -466,7 +466,7 @@ def _roofline(args, cfg, s, prec_name: str, prof: dict, peaks: dict, fp64_peak: 
                         "pipe slot, so the pipe is busier than this fraction"}
         c576 = dom == "xprod" and cfg.get("ngalx") == 576 and cfg.get("ngalz") == 576 and not cfg.get("ngalx2")
         if c576:
-            fp64["pipe_active_ncu"] = 0.848
+            fp64["pipe_active_ncu"] = 0.853
             fp64["pipe_active_src"] = ("profiles/k_xprod_xz576_fp64.txt: ncu sm__pipe_fp64_cycles_active of this "
                                        "kernel at configuration 2's transform lengths (a committed capture, not "
                                        "measured in this run)")
