@@ -252,9 +252,10 @@ int lh_profile_step(lh_handle* h, double* ms_by_kind, int32_t* count_by_kind, in
 /* Launch-shape autotuner (no reference counterpart).  Times the z passes for
  * each z tile width (columns per CTA) and the product pass for each number of
  * levels per CTA on this handle's grid and precision, keeps the fastest of
- * each, the z passes' and the product pass's threads per CTA and the product
- * pass's buffer split (read them back with lh_get_launch_shapes,
- * lh_get_z_threads and lh_get_x_threads), keeps the fastest of
+ * each, the z passes' and the product pass's threads per CTA, the product
+ * pass's buffer split and, in the mixed form, its rows per CTA (read them back
+ * with lh_get_launch_shapes, lh_get_z_threads, lh_get_x_threads and
+ * lh_get_x_rows), keeps the fastest of
  * each and returns the first two (either pointer may be NULL).  Needs fields; writes
  * only scratch, so the fields and the time are unchanged.  The next step is
  * captured with the new shapes. */
@@ -277,6 +278,12 @@ int lh_get_x_threads(lh_handle* h, int32_t* threads);
  * by timing at the z tile width it chose.  Batched ensemble launches always
  * use 256. */
 int lh_get_z_threads(lh_handle* h, int32_t* threads);
+
+/* z rows per product-pass CTA the next step uses (no reference counterpart):
+ * 2 when the mixed form runs two rows' FP32 transforms in lockstep (the same
+ * arithmetic per row, so the same results), else 1; lh_autotune picks it by
+ * timing.  Batched ensemble launches always use 1. */
+int lh_get_x_rows(lh_handle* h, int32_t* rows);
 
 
 /* Divergence-free projection (solveP + v_corr with kRK = 1, the operation of

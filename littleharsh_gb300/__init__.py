@@ -32,7 +32,7 @@ EXPORTED_SYMBOLS = [
     "lh_cfl_dt", "lh_project", "lh_spectra_accumulate", "lh_spectra_flush", "lh_stats_accumulate",
     "lh_stats_flush", "lh_cond_accumulate", "lh_cond_flush", "lh_last_step_ms", "lh_profile_step",
     "lh_project_noalloc", "lh_set_monitor", "lh_get_monitor", "lh_fp64_peak", "lh_ensemble_create", "lh_ensemble_step", "lh_ensemble_last_error",
-    "lh_ensemble_free", "lh_ensemble_set_mode", "lh_ensemble_info", "lh_autotune", "lh_get_launch_shapes", "lh_get_x_threads", "lh_get_z_threads", "lh_write_restart", "lh_read_restart", "lh_write_stats", "lh_write_spectra", "lh_read_input", "lh_setup_grid", "lh_setup_canopy",
+    "lh_ensemble_free", "lh_ensemble_set_mode", "lh_ensemble_info", "lh_autotune", "lh_get_launch_shapes", "lh_get_x_threads", "lh_get_z_threads", "lh_get_x_rows", "lh_write_restart", "lh_read_restart", "lh_write_stats", "lh_write_spectra", "lh_read_input", "lh_setup_grid", "lh_setup_canopy",
     # include/lh_srnet.h: kernels of the learned warm start
     "lh_sr_conv_fwd", "lh_sr_conv_fwd_tc", "lh_sr_tc_status", "lh_sr_conv_wgrad", "lh_sr_conv_wgrad_tc", "lh_sr_flip_weights", "lh_sr_mse", "lh_sr_adam",
 ]
@@ -130,6 +130,7 @@ def load_library(build: bool = True) -> C.CDLL:
     L.lh_get_launch_shapes.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]
     L.lh_get_x_threads.argtypes = [vp, C.POINTER(i32)]
     L.lh_get_z_threads.argtypes = [vp, C.POINTER(i32)]
+    L.lh_get_x_rows.argtypes = [vp, C.POINTER(i32)]
     L.lh_project_noalloc.argtypes = [C.POINTER(Params)] + [_dp] * 3 + [C.c_void_p] * 3 + [C.c_double, C.c_void_p]
     L.lh_write_restart.argtypes = [vp, C.POINTER(Params), _dp, _dp, cp, cp, i32]
     L.lh_read_restart.argtypes = [vp, cp, cp, _dp, C.POINTER(i32)]
@@ -366,12 +367,14 @@ class Solver:
     def launch_shapes(self) -> dict:
         """The z tile width, levels per product-pass CTA, product-pass buffer split and threads per
         product-pass and z-pass CTA in use."""
-        tx, ch, xs, xt, zt = (C.c_int32(0) for _ in range(5))
+        tx, ch, xs, xt, zt, xr = (C.c_int32(0) for _ in range(6))
         L = load_library()
         self._check(L.lh_get_launch_shapes(self.h, C.byref(tx), C.byref(ch), C.byref(xs)))
         self._check(L.lh_get_x_threads(self.h, C.byref(xt)))
         self._check(L.lh_get_z_threads(self.h, C.byref(zt)))
-        return {"tx": tx.value, "chunk": ch.value, "xsplit": xs.value, "xthreads": xt.value, "zthreads": zt.value}
+        self._check(L.lh_get_x_rows(self.h, C.byref(xr)))
+        return {"tx": tx.value, "chunk": ch.value, "xsplit": xs.value, "xthreads": xt.value, "zthreads": zt.value,
+                "xrows": xr.value}
 
     # diagnostics ------------------------------------------------------------
     def divmax(self) -> float:

@@ -83,6 +83,7 @@ struct lh_handle {
   int xsplit = 0;  // x-pass: face pair transformed on its own (smaller shared-memory footprint)
   int xthreads = 256;  // x-pass: threads per CTA (128 or 256)
   int zthreads = 256;  // z passes of the nonlinear term and the canopy forcing: threads per CTA (128 or 256)
+  int xrows = 1;       // x-pass: z rows per CTA (2: the mixed form's two-row lockstep kernel)
   // state
   double t_now = 0, dt = 0;
   bool have_fields = false, have_dt = false;
@@ -391,6 +392,7 @@ int nl_bands(const lh_handle* h, NlBand<R>* out) {
       a.wc = h->t.wc; a.wf = h->t.wf; a.dyc = h->t.dyc;
       a.dxi = db.ngx / h->Lx; a.dzi = db.ngz / h->Lz;
       a.sc = h->sc; a.want_cfl = 0; a.chunk = h->chunk; a.split = h->xsplit; a.threads = h->xthreads;
+      a.rows = (sizeof(R) == 4 && h->xrows == 2 && !h->xsplit && db.ngz % 2 == 0) ? 2 : 1;
       a.c_lo = B.c_lo; a.c_hi = B.c_hi; a.f_lo = B.f_lo; a.f_hi = B.f_hi;
       a.mean_split = sizeof(R) == 4;
       a.us = h->u1; a.ws = h->u3; a.nps = d.np;
@@ -970,6 +972,7 @@ int lh_init(const lh_params* prm, const double* yu, const double* yv, const doub
   if (const char* v = std::getenv("LH_XSPLIT")) h->xsplit = std::atoi(v) != 0 ? 1 : 0;
   if (const char* v = std::getenv("LH_XTHREADS")) h->xthreads = std::atoi(v) == 128 ? 128 : 256;
   if (const char* v = std::getenv("LH_ZTHREADS")) h->zthreads = std::atoi(v) == 128 ? 128 : 256;
+  if (const char* v = std::getenv("LH_XROWS")) h->xrows = std::atoi(v) == 2 ? 2 : 1;
   {
     const cudaError_t e = configure_kernels();
     if (e != cudaSuccess) return bail(fail(h, LH_ECUDA, "kernel attributes: %s", cudaGetErrorString(e)));
@@ -1283,10 +1286,12 @@ void build_batched(const std::vector<lh_handle*>& hs, std::vector<Slot>& slots) 
           dim3 g;
           size_t sm;
           if (part == 1) {
-            xprod_shape<R>(B.xp, *B.d, &g, &sm);
+            ProdArgs<R> xa = B.xp;
+            xa.rows = 1;  // the batched launch runs one z row per CTA
+            xprod_shape<R>(xa, *B.d, &g, &sm);
             if (g.x == 0) continue;
             XDesc<R> D{};
-            D.a = B.xp; D.d = *B.d; D.ph = *B.ph; D.pf = *B.pf; D.rtw = B.rtw; D.gx = g.x; D.gy = g.y;
+            D.a = xa; D.d = *B.d; D.ph = *B.ph; D.pf = *B.pf; D.rtw = B.rtw; D.gx = g.x; D.gy = g.y;
             xd.push_back(D);
           } else {
             const ZJobs<R>& J = part == 0 ? B.zi : B.zf;
@@ -1645,20 +1650,34 @@ int lh_autotune(lh_handle* h, int32_t* tx_out, int32_t* chunk_out) {
     h->xsplit = t2[1] < t2[0] ? 1 : 0;
     if (h->xsplit != xs0 && h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; ++h->graph_gen; }
   }
-  // threads per x-pass CTA: the transforms' stages have 100-200 butterflies, so 128 threads with twice the
-  // CTAs per SM can beat 256
+  // threads per x-pass CTA (the transforms' stages have 100-200 butterflies, so 128 threads with twice the
+  // CTAs per SM can beat 256) and, in the mixed form without the split, one or two z rows per CTA (the
+  // two-row pass runs both rows' FP32 transforms in lockstep with the same arithmetic per row); both chosen
+  // together, since the best block size depends on the rows per CTA
   {
-    const int xt0 = h->xthreads;
-    float t2[2] = {0.f, 0.f};
-    const int cand[2] = {256, 128};
-    for (int c = 0; c < 2; ++c) {
-      h->xthreads = cand[c];
-      t2[c] = h->precision == LH_PREC_MIXED ? time_parts<float>(h, false, true, e0, e1)
-                                            : time_parts<double>(h, false, true, e0, e1);
-      if (t2[c] < 0.f) { h->xthreads = xt0; cudaEventDestroy(e0); cudaEventDestroy(e1); return fail(h, LH_ECUDA, "autotune: product pass failed"); }
+    const int xt0 = h->xthreads, xr0 = h->xrows;
+    const int maxrows = (h->precision == LH_PREC_MIXED && !h->xsplit) ? 2 : 1;
+    float bestx = 1e30f;
+    int bt = xt0, br = 1;
+    for (int r = 1; r <= maxrows; ++r) {
+      for (int th : {256, 128}) {
+        h->xrows = r;
+        h->xthreads = th;
+        const float ms = h->precision == LH_PREC_MIXED ? time_parts<float>(h, false, true, e0, e1)
+                                                       : time_parts<double>(h, false, true, e0, e1);
+        if (ms < 0.f) {
+          h->xthreads = xt0; h->xrows = xr0;
+          cudaEventDestroy(e0); cudaEventDestroy(e1);
+          return fail(h, LH_ECUDA, "autotune: product pass failed");
+        }
+        if (ms < bestx) { bestx = ms; bt = th; br = r; }
+      }
     }
-    h->xthreads = t2[1] < t2[0] ? 128 : 256;
-    if (h->xthreads != xt0 && h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; ++h->graph_gen; }
+    h->xthreads = bt;
+    h->xrows = br;
+    if ((h->xthreads != xt0 || h->xrows != xr0) && h->graph) {
+      cudaGraphExecDestroy(h->graph); h->graph = nullptr; ++h->graph_gen;
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -1683,6 +1702,12 @@ int lh_get_launch_shapes(lh_handle* h, int32_t* tx, int32_t* chunk, int32_t* xsp
 int lh_get_x_threads(lh_handle* h, int32_t* threads) {
   if (!h || !threads) return LH_EINVAL;
   *threads = h->xthreads;
+  return LH_OK;
+}
+
+int lh_get_x_rows(lh_handle* h, int32_t* rows) {
+  if (!h || !rows) return LH_EINVAL;
+  *rows = (h->precision == LH_PREC_MIXED && h->xrows == 2 && !h->xsplit) ? 2 : 1;
   return LH_OK;
 }
 

@@ -252,6 +252,54 @@ __device__ __forceinline__ void dit_stage_padded(cpx_t<R>* buf, int nb, int bs, 
   }
 }
 
+// Two FP32 x transforms in lockstep: element i of a float4 buffer holds sample i of one transform in (x, y)
+// and of another in (z, w), in the padded slots of sxi<float>.  A thread runs the same butterfly of both with
+// the arithmetic of dit_stage_padded, so each half comes out bit for bit as the one-transform path computes
+// it, while the index arithmetic, the twiddle loads and the shared-memory instructions serve both.
+__device__ __forceinline__ float2 lo2(float4 v) { return float2{v.x, v.y}; }
+__device__ __forceinline__ float2 hi2(float4 v) { return float2{v.z, v.w}; }
+__device__ __forceinline__ float4 cat4(float2 a, float2 b) { return float4{a.x, a.y, b.x, b.y}; }
+
+template <int SIGN, int RADIX>
+__device__ __forceinline__ void dit_stage_padded2(float4* buf, int nb, int bs, int L, int n, unsigned mm,
+                                                  unsigned nbfm, const float2* __restrict__ tw) {
+  const int m = L / RADIX, ts = n / L;
+  const int nbf = n / RADIX;
+  const int total = nb * nbf;
+  const bool twiddle = m > 1;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int b = fdiv(t, nbf, nbfm), f = t - b * nbf;
+    const int blk = fdiv(f, m, mm), k = f - blk * m;
+    const int i0 = b * bs + blk * L + k;
+    float2 va[RADIX], vb[RADIX];
+#pragma unroll
+    for (int p = 0; p < RADIX; ++p) {
+      const float4 q = buf[sxi<float>(i0 + p * m)];
+      va[p] = lo2(q);
+      vb[p] = hi2(q);
+    }
+    bfly<float, SIGN, RADIX>(va, k * ts, twiddle, false, tw);
+    bfly<float, SIGN, RADIX>(vb, k * ts, twiddle, false, tw);
+#pragma unroll
+    for (int p = 0; p < RADIX; ++p) buf[sxi<float>(i0 + p * m)] = cat4(va[p], vb[p]);
+  }
+}
+
+// The DIT stages of plan P over nb float4 vectors (vector b at buf[b*bs]), input at digit-reversed positions.
+template <int SIGN>
+__device__ void fft_dit2(float4* buf, int nb, int bs, const FftPlan& P) {
+  const float2* __restrict__ tw = P.tw32;
+  const int n = P.n;
+  for (int s = 0; s < P.ns; ++s) {
+    const int r = P.rad[s], L = P.len[s];
+    const unsigned mm = P.mdiv[s], nbfm = P.qdiv[s];
+    if (r == 4) dit_stage_padded2<SIGN, 4>(buf, nb, bs, L, n, mm, nbfm, tw);
+    else if (r == 2) dit_stage_padded2<SIGN, 2>(buf, nb, bs, L, n, mm, nbfm, tw);
+    else dit_stage_padded2<SIGN, 3>(buf, nb, bs, L, n, mm, nbfm, tw);
+    __syncthreads();
+  }
+}
+
 // In-place DIT over `nb` vectors: element e of vector b at buf[b*bs + e*es].
 // BFAST: consecutive threads take consecutive vectors (for interleaved
 // vectors, es = nb-ish, bs = 1); otherwise consecutive butterflies of one

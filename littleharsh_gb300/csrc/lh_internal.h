@@ -154,6 +154,8 @@ struct ProdArgs {
   int chunk;
   int split;            // 1: the face pair is transformed after the centre pairs, through two buffer vectors
   int threads;          // threads per CTA of the stand-alone launch (128 or 256; the batched launch uses 256)
+  int rows;             // z rows per CTA of the stand-alone launch: 2 runs two rows' transforms in lockstep
+                        // (FP32, unsplit, ngz even; the same arithmetic per row); otherwise 1
   // levels this launch forms products on (a band's planes): centres c_lo..c_hi, faces f_lo..f_hi
   int c_lo, c_hi, f_lo, f_hi;
   // mixed form: mu, mw hold the fluctuations u' = u - U(y), w' = w - W(y) (the z-inverse left the (0,0) modes

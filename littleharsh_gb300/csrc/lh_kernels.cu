@@ -414,10 +414,235 @@ __global__ void __launch_bounds__(256) k_xprod(const __grid_constant__ ProdArgs<
   xprod_body<R>(a, d, ph, pf, rtw, blockIdx.x, blockIdx.y);
 }
 
+// ---- the FP32 product pass on two z rows per CTA --------------------------------------------------------
+// The same work as xprod_body for the rows 2 bx and 2 bx + 1, their transforms run in lockstep (fft_dit2):
+// element x of a float4 transform buffer holds row 0's complex sample in (x, y) and row 1's in (z, w), and a
+// physical row keeps both rows' values as float2 pairs.  Every per-row operation is the one xprod_body does,
+// in the same order, so the results are the same bit for bit; the index arithmetic, twiddle and permutation
+// loads and shared-memory instructions of a butterfly or an element serve both rows.
+
+// xprod_body's x_inverse_pair for two rows: z = a + i b of row q in the q-th half of each element
+__device__ void x_inverse_pair2(const float2* rowA0, const float2* rowB0, const float2* rowA1, const float2* rowB1,
+                                float4* F, float2* outA, float2* outB, const Dims& d, const FftPlan& pf) {
+  const int n = d.ngx, nkx = d.nkx;
+  auto pack = [&](const float2* rowA, const float2* rowB, int k) {
+    float2 z = float2{0.f, 0.f};
+    if (k == 0) {
+      z = float2{rowA[0].x, rowB[0].x};
+    } else if (k < nkx) {
+      const float2 a = rowA[k], b = rowB[k];
+      z = float2{a.x - b.y, a.y + b.x};
+    } else if (k > n - nkx) {
+      const float2 a = rowA[n - k], b = rowB[n - k];
+      z = float2{a.x + b.y, b.x - a.y};
+    }
+    return z;
+  };
+  for (int k = threadIdx.x; k < n; k += blockDim.x)
+    F[sxi<float>(pf.perm[k])] = cat4(pack(rowA0, rowB0, k), pack(rowA1, rowB1, k));
+  __syncthreads();
+  fft_dit2<+1>(F, 1, n, pf);
+  for (int x = threadIdx.x; x < n; x += blockDim.x) {
+    const float4 z = F[sxi<float>(x)];
+    outA[x] = float2{z.x, z.z};
+    outB[x] = float2{z.y, z.w};
+  }
+  __syncthreads();
+}
+
+// xprod_body's half-length inverse of one v row, for two rows
+__device__ void x_inverse2(const float2* row0, const float2* row1, float4* F, float2* out, const Dims& d,
+                           const FftPlan& ph, const double2* __restrict__ rtw) {
+  const int h = d.ngx / 2, nkx = d.nkx;
+  auto pre = [&](const float2* row, int k, float wr, float wi) {
+    float2 a = (k < nkx) ? row[k] : float2{0.f, 0.f};
+    if (k == 0) a.y = 0.f;
+    const int k2 = h - k;
+    float2 b = (k > 0 && k2 < nkx) ? row[k2] : float2{0.f, 0.f};
+    b.y = -b.y;
+    const float2 s = cadd(a, b), df = csub(a, b);
+    const float2 q = float2{wr * df.x - wi * df.y, wr * df.y + wi * df.x};
+    return float2{s.x - q.y, s.y + q.x};
+  };
+  for (int k = threadIdx.x; k < h; k += blockDim.x) {
+    const double2 w = rtw[k];
+    const float wr = (float)w.x, wi = (float)-w.y;  // exp(+2 pi i k/n)
+    F[sxi<float>(ph.perm[k])] = cat4(pre(row0, k, wr, wi), pre(row1, k, wr, wi));
+  }
+  __syncthreads();
+  fft_dit2<+1>(F, 1, h + 1, ph);
+  for (int m = threadIdx.x; m < h; m += blockDim.x) {
+    const float4 z = F[sxi<float>(m)];
+    out[2 * m] = float2{z.x, z.z};
+    out[2 * m + 1] = float2{z.y, z.w};
+  }
+  __syncthreads();
+}
+
+// xprod_body's x_forward_pairs for two rows: np2 packed pairs into rows0[2p], rows0[2p+1] (row 0) and
+// rows1[2p], rows1[2p+1] (row 1)
+__device__ void x_forward_pairs2(int np2, float4* F, float2* const* rows0, float2* const* rows1, const Dims& d,
+                                 const FftPlan& pf) {
+  const int n = d.ngx, nkx = d.nkx;
+  const float sc = (float)(0.5 / n);
+  fft_dit2<-1>(F, np2, n, pf);
+  for (int e = threadIdx.x; e < np2 * nkx; e += blockDim.x) {
+    const int p = e / nkx, k = e - p * nkx;
+    const float4 zk4 = F[sxi<float>(p * n + k)];
+    const float4 zc4 = F[sxi<float>(p * n + ((n - k) % n))];
+    const float2 zk0 = lo2(zk4), zc0 = lo2(zc4), zk1 = hi2(zk4), zc1 = hi2(zc4);
+    rows0[2 * p][k] = float2{sc * (zk0.x + zc0.x), sc * (zk0.y - zc0.y)};
+    rows0[2 * p + 1][k] = float2{sc * (zk0.y + zc0.y), sc * (zc0.x - zk0.x)};
+    rows1[2 * p][k] = float2{sc * (zk1.x + zc1.x), sc * (zk1.y - zc1.y)};
+    rows1[2 * p + 1][k] = float2{sc * (zk1.y + zc1.y), sc * (zc1.x - zk1.x)};
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void xprod2_body(const ProdArgs<float>& a, const Dims& d, const FftPlan& ph,
+                                            const FftPlan& pf, const double2* __restrict__ rtw, int bx, int by) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int ngx = d.ngx;
+  float4* F = reinterpret_cast<float4*>(smraw);  // 3 vectors of ngx
+  float2* rowsm = reinterpret_cast<float2*>(F + sx_elems<float>(3 * (size_t)ngx));  // 6 rows of ngx pairs
+  float2* up = rowsm;
+  float2* wp = rowsm + ngx;
+  float2* vp = rowsm + 2 * ngx;
+  float2* uc = rowsm + 3 * ngx;
+  float2* wc = rowsm + 4 * ngx;
+  float2* vc = rowsm + 5 * ngx;
+  __shared__ double cflred[8];
+  const int kz0 = 2 * bx;
+  const int L0 = min(a.c_lo, a.f_lo + 1), L1 = max(a.c_hi, a.f_hi + 1);
+  const int c0 = L0 + by * a.chunk;
+  const int c1 = min(c0 + a.chunk - 1, L1);
+  if (c0 > c1) return;
+  const size_t ro0 = (size_t)kz0 * d.nkx, ro1 = ro0 + d.nkx;
+  double cmax = 0.0;
+  auto inverse = [&](int lev, float2* ou, float2* ow) {
+    const size_t o = (size_t)lev * d.mp;
+    x_inverse_pair2(a.mu + o + ro0, a.mw + o + ro0, a.mu + o + ro1, a.mw + o + ro1, F, ou, ow, d, pf);
+  };
+  if (c0 - 1 >= 1) {
+    inverse(c0 - 1, up, wp);
+    const size_t o = (size_t)(c0 - 1) * d.mp;
+    x_inverse2(a.mv + o + ro0, a.mv + o + ro1, F, vp, d, ph, rtw);
+  } else {
+    for (int x = threadIdx.x; x < 3 * ngx; x += blockDim.x) up[x] = float2{0.f, 0.f};
+    __syncthreads();
+  }
+  for (int jj = c0; jj <= c1; ++jj) {
+    const bool vface = jj <= d.nyv - 2;
+    inverse(jj, uc, wc);
+    if (vface) {
+      const size_t o = (size_t)jj * d.mp;
+      x_inverse2(a.mv + o + ro0, a.mv + o + ro1, F, vc, d, ph, rtw);
+    } else {
+      for (int x = threadIdx.x; x < ngx; x += blockDim.x) vc[x] = float2{0.f, 0.f};
+      __syncthreads();
+    }
+    const bool cprod = jj >= a.c_lo && jj <= a.c_hi;
+    const bool fprod = jj - 1 >= a.f_lo && jj - 1 <= a.f_hi;
+    const float wcj = (float)a.wc[jj];
+    const float wfj = fprod ? (float)a.wf[jj - 1] : 0.f;
+    const double dyi = a.dyc[jj];
+    const int fslot = cprod ? 2 : 0;
+    float Uc = 0.f, Wc = 0.f, Uf = 0.f, Wf = 0.f;
+    if (a.mean_split) {
+      const float Um = (float)a.us[(size_t)(jj - 1) * a.nps].x, Wm = (float)a.ws[(size_t)(jj - 1) * a.nps].x;
+      Uc = (float)a.us[(size_t)jj * a.nps].x;
+      Wc = (float)a.ws[(size_t)jj * a.nps].x;
+      Uf = Um + wfj * (Uc - Um);
+      Wf = Wm + wfj * (Wc - Wm);
+    }
+    for (int x = threadIdx.x; x < ngx; x += blockDim.x) {
+      const float2 u2 = uc[x], w2 = wc[x];
+      const int px = pf.perm[x];
+      const float us[2] = {u2.x, u2.y}, ws[2] = {w2.x, w2.y};
+      if (cprod) {
+        const float2 vp2 = vp[x], vc2 = vc[x];
+        const float vps[2] = {vp2.x, vp2.y}, vcs[2] = {vc2.x, vc2.y};
+        float2 p0[2], p1[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const float u = us[q], w = ws[q];
+          const float v = vps[q] + wcj * (vcs[q] - vps[q]);
+          p0[q] = float2{u * ((Uc + Uc) + u), u * (Wc + w) + Uc * w};
+          p1[q] = float2{w * ((Wc + Wc) + w), v * v};
+          if (a.want_cfl) {
+            const double cv = fabs((double)u) * a.dxi + fabs((double)v) * dyi + fabs((double)w) * a.dzi;
+            cmax = fmax(cmax, cv);
+          }
+        }
+        F[sxi<float>(px)] = cat4(p0[0], p0[1]);
+        F[sxi<float>(ngx + px)] = cat4(p1[0], p1[1]);
+      }
+      if (fprod) {
+        const float2 up2 = up[x], wp2 = wp[x], vp2 = vp[x];
+        const float ups[2] = {up2.x, up2.y}, wps[2] = {wp2.x, wp2.y}, vps[2] = {vp2.x, vp2.y};
+        float2 pf2[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const float uf = ups[q] + wfj * (us[q] - ups[q]);
+          const float wf = wps[q] + wfj * (ws[q] - wps[q]);
+          pf2[q] = float2{(Uf + uf) * vps[q], (Wf + wf) * vps[q]};
+        }
+        F[sxi<float>(fslot * ngx + px)] = cat4(pf2[0], pf2[1]);
+      }
+    }
+    __syncthreads();
+    if (cprod || fprod) {
+      float2* rows0[6];
+      float2* rows1[6];
+      int npair = 0;
+      if (cprod) {
+        for (int q = 0; q < 4; ++q) {
+          rows0[q] = a.out[q] + (size_t)jj * d.mp + ro0;
+          rows1[q] = a.out[q] + (size_t)jj * d.mp + ro1;
+        }
+        npair = 2;
+      }
+      if (fprod) {
+        rows0[2 * npair] = a.out[4] + (size_t)(jj - 1) * d.mp + ro0;
+        rows0[2 * npair + 1] = a.out[5] + (size_t)(jj - 1) * d.mp + ro0;
+        rows1[2 * npair] = a.out[4] + (size_t)(jj - 1) * d.mp + ro1;
+        rows1[2 * npair + 1] = a.out[5] + (size_t)(jj - 1) * d.mp + ro1;
+        ++npair;
+      }
+      x_forward_pairs2(npair, F, rows0, rows1, d, pf);
+    }
+    float2* t;
+    t = up; up = uc; uc = t;
+    t = wp; wp = wc; wc = t;
+    t = vp; vp = vc; vc = t;
+  }
+  if (a.want_cfl) {
+    for (int o = 16; o > 0; o >>= 1) cmax = fmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, o));
+    if ((threadIdx.x & 31) == 0) cflred[threadIdx.x >> 5] = cmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double m = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, cflred[w]);
+      atomicMax(&a.sc->cflbits, (unsigned long long)__double_as_longlong(m));
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_xprod2(const __grid_constant__ ProdArgs<float> a,
+                                                const __grid_constant__ Dims d, const __grid_constant__ FftPlan ph,
+                                                const __grid_constant__ FftPlan pf, const double2* __restrict__ rtw) {
+  xprod2_body(a, d, ph, pf, rtw, blockIdx.x, blockIdx.y);
+}
+
 template <typename R>
 void xprod_shape(const ProdArgs<R>& a, const Dims& d, dim3* grid, size_t* smem) {
   const int L0 = std::min(a.c_lo, a.f_lo + 1), L1 = std::max(a.c_hi, a.f_hi + 1);
   const int nlev = L1 - L0 + 1;
+  if (sizeof(R) == 4 && a.rows == 2) {
+    *grid = nlev <= 0 ? dim3(0, 0, 0) : dim3(d.ngz / 2, (nlev + a.chunk - 1) / a.chunk);
+    *smem = sizeof(float4) * sx_elems<float>(3 * (size_t)d.ngx) + sizeof(float2) * 6 * (size_t)d.ngx;
+    return;
+  }
   *grid = nlev <= 0 ? dim3(0, 0, 0) : dim3(d.ngz, (nlev + a.chunk - 1) / a.chunk);
   *smem = sizeof(cpx_t<R>) * sx_elems<R>((a.split ? 2 : 3) * (size_t)d.ngx) + sizeof(R) * 6 * (size_t)d.ngx;
 }
@@ -429,6 +654,12 @@ void launch_xprod(const ProdArgs<R>& a, const Dims& d, const FftPlan& ph, const 
   size_t sm;
   xprod_shape(a, d, &grid, &sm);
   if (grid.x == 0) return;
+  if constexpr (sizeof(R) == 4) {
+    if (a.rows == 2) {
+      k_xprod2<<<grid, a.threads == 128 ? 128 : 256, sm, st>>>(a, d, ph, pf, rtw);
+      return;
+    }
+  }
   k_xprod<R><<<grid, a.threads == 128 ? 128 : 256, sm, st>>>(a, d, ph, pf, rtw);
 }
 
@@ -1437,9 +1668,9 @@ cudaError_t configure_kernels() {
   int optin = 0;
   e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e != cudaSuccess) return e;
-  const cudaError_t r[17] = {allow_smem(k_xcond, optin), allow_smem(k_zinv<double>, optin), allow_smem(k_zinv<float>, optin),
+  const cudaError_t r[18] = {allow_smem(k_xcond, optin), allow_smem(k_zinv<double>, optin), allow_smem(k_zinv<float>, optin),
                              allow_smem(k_zfwd<double>, optin), allow_smem(k_zfwd<float>, optin),
-                             allow_smem(k_xprod<double>, optin), allow_smem(k_xprod<float>, optin),
+                             allow_smem(k_xprod<double>, optin), allow_smem(k_xprod<float>, optin), allow_smem(k_xprod2, optin),
                              allow_smem(k_xmask<double>, optin), allow_smem(k_xmask<float>, optin),
                              allow_smem(k_zinv_batch<double>, optin), allow_smem(k_zinv_batch<float>, optin),
                              allow_smem(k_zfwd_batch<double>, optin), allow_smem(k_zfwd_batch<float>, optin),

@@ -172,7 +172,7 @@ def test_autotune_keeps_results(oracle_mod):
     t.set_time(0.0, tm["dt"], 0.0, tm["QxT"])
     shapes = t.autotune()
     assert shapes["tx"] in (1, 2, 4, 8, 16, 32) and shapes["chunk"] in (4, 8, 16, 32, 64)
-    assert shapes["xthreads"] in (128, 256) and shapes["zthreads"] in (128, 256)
+    assert shapes["xthreads"] in (128, 256) and shapes["zthreads"] in (128, 256) and shapes["xrows"] == 1
     s.step(3)
     t.step(3)
     for a, b in zip(t.get_fields(), s.get_fields()):
@@ -212,6 +212,25 @@ def test_pass_threads_keep_results(oracle_mod, monkeypatch, mixed, which):
         monkeypatch.setenv(f"LH_{which.upper()}THREADS", threads)
         s = lh.Solver(lh.Config(**C1), precision=prec)
         assert s.launch_shapes()[f"{which}threads"] == int(threads)
+        s.set_fields(*s0.get_fields())
+        tm = s0.time()
+        s.set_time(0.0, tm["dt"], 0.0, tm["QxT"])
+        s.step(3)
+        sols.append(s)
+    for a, b in zip(sols[0].get_fields(), sols[1].get_fields()):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_two_row_product_pass_keeps_results(oracle_mod, monkeypatch):
+    """The mixed form's product pass with two z rows per CTA runs each row's transforms, products and
+    truncation with the arithmetic of the one-row pass: bit for bit the same steps."""
+    import littleharsh_gb300 as lh
+    o, s0 = _pair(oracle_mod, C1)
+    sols = []
+    for rows in ("1", "2"):
+        monkeypatch.setenv("LH_XROWS", rows)
+        s = lh.Solver(lh.Config(**C1), precision=lh.PREC_MIXED)
+        assert s.launch_shapes()["xrows"] == int(rows)
         s.set_fields(*s0.get_fields())
         tm = s0.time()
         s.set_time(0.0, tm["dt"], 0.0, tm["QxT"])
