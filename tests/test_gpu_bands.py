@@ -95,3 +95,22 @@ def test_band_mixed_precision_close(oracle_mod):
     s.step(10)
     for a, b in zip(s.get_fields(), o.get_fields()):
         assert rel_l2(a, b) < 1e-4
+
+
+def test_two_row_product_pass_with_bands(oracle_mod, monkeypatch):
+    """The mixed form's two-row product pass on every band (the fine bands' 48-point rows and the middle
+    band's 24-point rows): bit for bit the one-row steps."""
+    import littleharsh_gb300 as lh
+    o, s0 = _pair(oracle_mod, BAND48, precision=lh.PREC_MIXED)
+    sols = []
+    for rows in ("1", "2"):
+        monkeypatch.setenv("LH_XROWS", rows)
+        s = lh.Solver(lh.Config(**BAND48), precision=lh.PREC_MIXED)
+        assert s.launch_shapes()["xrows"] == int(rows)
+        s.set_fields(*s0.get_fields())
+        tm = s0.time()
+        s.set_time(0.0, tm["dt"], 0.0, tm["QxT"])
+        s.step(3)
+        sols.append(s)
+    for a, b in zip(sols[0].get_fields(), sols[1].get_fields()):
+        np.testing.assert_array_equal(a, b)
