@@ -249,16 +249,17 @@ int lh_last_step_ms(lh_handle* h, double* ms, int32_t* launches_per_step);
  * nkinds must be at least 10. */
 int lh_profile_step(lh_handle* h, double* ms_by_kind, int32_t* count_by_kind, int32_t nkinds);
 
-/* Launch-shape autotuner (no reference counterpart).  Times the z passes for
- * each z tile width (columns per CTA) and the product pass for each number of
- * levels per CTA on this handle's grid and precision, keeps the fastest of
- * each, the z passes' and the product pass's threads per CTA, the product
- * pass's buffer split and, in the mixed form, its rows per CTA (read them back
- * with lh_get_launch_shapes, lh_get_z_threads, lh_get_x_threads and
- * lh_get_x_rows), keeps the fastest of
- * each and returns the first two (either pointer may be NULL).  Needs fields; writes
- * only scratch, so the fields and the time are unchanged.  The next step is
- * captured with the new shapes. */
+/* Launch-shape autotuner (no reference counterpart).  On this handle's grid
+ * and precision it times, in turn, the z passes for each z tile width
+ * (columns per CTA) and then for 128 and 256 threads per CTA, the product pass
+ * for each number of levels per CTA, its buffer split, and its threads per CTA
+ * together with (in the mixed form) one or two z rows per CTA; it keeps the
+ * fastest of each and returns the tile width and the levels per CTA (either
+ * pointer may be NULL; read the rest back with lh_get_launch_shapes,
+ * lh_get_z_threads, lh_get_x_threads and lh_get_x_rows).  Needs fields; writes
+ * only scratch, so the fields and the time are unchanged, and every choice
+ * gives the same results bit for bit.  The next step is captured with the new
+ * shapes. */
 int lh_autotune(lh_handle* h, int32_t* tx, int32_t* chunk);
 
 /* The launch shapes the next step uses (no reference counterpart): z tile
@@ -284,7 +285,6 @@ int lh_get_z_threads(lh_handle* h, int32_t* threads);
  * arithmetic per row, so the same results), else 1; lh_autotune picks it by
  * timing.  Batched ensemble launches always use 1. */
 int lh_get_x_rows(lh_handle* h, int32_t* rows);
-
 
 /* Divergence-free projection (solveP + v_corr with kRK = 1, the operation of
  * lh_project) of caller-owned device arrays u1, u2, u3 (plane layout), for
